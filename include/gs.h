@@ -1,0 +1,186 @@
+/*
+ * gs.h -- C ABI of the GB300 splat pipeline (libwebgs.so).
+ *
+ * Drop-in boundary for the reference's JavaScript Renderer (KoS-Y1/Web-GS-Renderer,
+ * src/renderer/renderer.js) and the WebGPU passes it encodes. Every entry point below names the
+ * reference interface it replaces. Plain C types only; nothing throws across the ABI; every call
+ * returns a status code (GS_OK = 0). One CUDA stream per context; a context is not thread-safe,
+ * separate contexts are independent.
+ */
+#ifndef WEBGS_GS_H
+#define WEBGS_GS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference reports through fail() dialogs and device-lost handlers,
+ *      src/utils/utils.js:3-47, src/gpu/device.js:30-35) ---------------------------------------- */
+#define GS_OK 0
+#define GS_ERR_INVALID 1   /* bad argument: null pointer, size out of range, unknown option */
+#define GS_ERR_OOM 2       /* device or pinned host allocation failed */
+#define GS_ERR_OVERFLOW 3  /* instances exceeded max_instance: output written, truncated exactly as
+                              emit.wgsl:57-59 truncates (a soft error) */
+#define GS_ERR_TIMEOUT 4   /* a device-side wait hit its iteration limit; results are invalid */
+#define GS_ERR_CUDA 5      /* a CUDA runtime call failed; gs_last_error() has the message */
+#define GS_ERR_STATE 6     /* call out of order, e.g. backward without a matching forward */
+#define GS_ERR_UNSUPPORTED 7
+
+/* ---- memory location of caller buffers -------------------------------------------------------- */
+#define GS_MEM_HOST 0      /* pageable or pinned host memory; the call is synchronous */
+#define GS_MEM_DEVICE 1    /* device memory of the context's GPU; the call is stream-ordered */
+
+/* ---- context flags ---------------------------------------------------------------------------- */
+#define GS_FLAG_PROFILE 1u /* record per-pass CUDA events (the reference's GpuProfiler,
+                              src/gpu/profiler.js:47-124) */
+#define GS_FLAG_NO_GRAPH 2u /* launch kernels one by one instead of replaying a CUDA graph */
+#define GS_FLAG_DIFFERENTIABLE 4u /* keep rgb, final T and last contributor of the last frame for
+                                     gs_backward (costs 20 bytes per pixel of extra writes) */
+
+/* GlobalUniforms (src/shaders/preprocess.wgsl:2-12), packed by renderer.js:773-797: 176 bytes,
+ * f32 offsets view@0, viewProj@16, eye@32, count(u32)@35, focal@36, tanFov@38, size@40. */
+typedef struct gs_view {
+    float view[16];       /* column-major view matrix (camera looks down -z) */
+    float view_proj[16];  /* projection * view, clip depth in [0, 1] */
+    float camera_pos[3];
+    uint32_t count;       /* ignored: the scene's count is used */
+    float focal[2];       /* W / (2 tanFovX), H / (2 tanFovY) */
+    float tan_fov[2];
+    float texture_size[2];/* image width, height in pixels (as floats) */
+    uint32_t pad0, pad1;
+} gs_view;
+
+/* Tunables. Defaults are the reference's constants (renderer.js:16-26). */
+typedef struct gs_config {
+    uint32_t tile_size;           /* 16 (reference); 8 and 32 also supported */
+    uint32_t digit_bits;          /* radix digit width: 8 (reference) or 4 */
+    uint32_t raster_batch;        /* splats staged per raster batch: 32, 64, 128 or 256 */
+    uint32_t max_instance_factor; /* instance budget per Gaussian (MAX_INSTANCE_FACTOR = 64) */
+    uint32_t flags;               /* GS_FLAG_* */
+    int32_t device;               /* CUDA device ordinal */
+} gs_config;
+
+/* Frame outputs. Any pointer may be NULL. All non-NULL pointers live in `location`. */
+typedef struct gs_image {
+    int32_t location;      /* GS_MEM_HOST or GS_MEM_DEVICE */
+    uint8_t* rgba8;        /* W*H*4: rgba8unorm (raseter.wgsl:115), alpha 255 */
+    float* rgb;            /* W*H*3: fp32 colour before quantization, pixel-interleaved */
+    float* final_t;        /* W*H: transmittance left after the last blended splat */
+    uint32_t* n_contrib;   /* W*H: contributor count at the last blended splat (raseter.wgsl:47,102) */
+} gs_image;
+
+/* Counters of the last frame (read back on request only; the reference never reads them). */
+typedef struct gs_frame_info {
+    uint32_t instance_count; /* I: sum of tilesTouched (offset_scan.wgsl:66) */
+    uint32_t sorted_count;   /* min(I, max_instance) (indirect_arg.wgsl:16) */
+    uint32_t max_instance;
+    uint32_t visible;        /* Gaussians with tilesTouched > 0 */
+    uint32_t near_pass;      /* Gaussians in front of the near plane (preprocess.wgsl:83) */
+    uint32_t tiles_x, tiles_y;
+    uint32_t status;         /* device status word: GS_DEV_* bits */
+    uint32_t sort_passes;
+} gs_frame_info;
+
+#define GS_DEV_OVERFLOW 1u
+#define GS_DEV_TIMEOUT 2u
+
+/* Intermediate buffers of the last frame, copied to host for parity checks. Any pointer may be
+ * NULL. Sizes: N = scene count, T = tiles_x * tiles_y, capacity = entries of keys/vals. */
+typedef struct gs_debug {
+    uint32_t* tiles_touched; /* N */
+    uint32_t* meta;          /* 4N: ((minY<<16)|minX, (maxY<<16)|maxX, depth16, 0) */
+    float* conic_opacity;    /* 4N */
+    float* pixel;            /* 2N */
+    float* color;            /* 4N (vec3f at a 16-byte stride) */
+    uint32_t* offsets;       /* N+1 */
+    uint32_t* keys;          /* capacity: sorted keys */
+    uint32_t* vals;          /* capacity: sorted Gaussian indices */
+    uint64_t capacity;
+    uint32_t* ranges;        /* 2T */
+} gs_debug;
+
+/* Per-pass timing row (the reference's profiler rows {label: {ms}}, profiler.js:113-121). */
+typedef struct gs_timing {
+    char label[24];
+    float ms;
+} gs_timing;
+
+typedef struct gs_ctx gs_ctx;
+typedef struct gs_scene gs_scene;
+
+/* ---- library --------------------------------------------------------------------------------- */
+const char* gs_version(void);
+void gs_config_default(gs_config* cfg);
+
+/* Replaces `new Renderer(device, context, format, onProfile)` (renderer.js:160-459) and the
+ * WebGPU device request (src/gpu/device.js:3-39). */
+int gs_ctx_create(const gs_config* cfg, gs_ctx** out);
+int gs_ctx_destroy(gs_ctx* ctx);
+/* Message of the last failed call on this context (static string on NULL ctx). */
+const char* gs_last_error(const gs_ctx* ctx);
+/* Blocks until the context's stream is idle; returns a pending device status (timeout). */
+int gs_ctx_synchronize(gs_ctx* ctx);
+/* The context's cudaStream_t, for callers that order their own work against it. */
+void* gs_ctx_stream(gs_ctx* ctx);
+
+/* Replaces Renderer.uploadGsData(data, name) (renderer.js:468-479): copies `packed` (59*count
+ * floats in the layout of preprocess.wgsl:16-24 / loader.js:75-85) to the device. The caller keeps
+ * ownership of `packed`; the scene owns its device copy. location: GS_MEM_HOST or GS_MEM_DEVICE. */
+int gs_scene_upload(gs_ctx* ctx, const float* packed, uint32_t count, int32_t location, gs_scene** out);
+/* Overwrites the attributes of an existing scene (same count), e.g. after an optimizer step. */
+int gs_scene_update(gs_ctx* ctx, gs_scene* scene, const float* packed, int32_t location);
+int gs_scene_destroy(gs_scene* scene);
+uint32_t gs_scene_count(const gs_scene* scene);
+
+/* Replaces Renderer.execute() (renderer.js:481-508) with the passes of renderer.js:822-932:
+ * preprocess, offset scan, emit, device-side sizing, radix sort, tile ranges, raster; the blit
+ * (blit.wgsl) becomes `out`. Host outputs: returns after the image is on the host. Device
+ * outputs: stream-ordered, returns after launch. Returns GS_ERR_OVERFLOW (outputs written) when
+ * the instance count exceeded the budget. */
+int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs_image* out);
+
+/* Counters of the last forward (synchronizes). */
+int gs_get_frame_info(gs_ctx* ctx, gs_frame_info* info);
+/* Intermediates of the last forward, copied to host (synchronizes). */
+int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg);
+
+/* Backward of the last gs_forward on `scene` (no counterpart in the reference, which is
+ * forward-only): dL_drgb is W*H*3 floats (gradient w.r.t. the fp32 rgb image); grad receives
+ * 59*count floats in the packed input layout. Both in `location`. */
+int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location);
+
+/* Per-pass timings of the last profiled frame (GS_FLAG_PROFILE); *n_rows receives the count. */
+int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_rows);
+
+/* ---- building blocks, exposed for parity tests on arbitrary inputs ---------------------------- */
+/* Stable LSD radix sort of (key, value) pairs on the low `key_bits` bits with the context's digit
+ * width (radix_parallel.wgsl:26-160). In place; keys/vals in `location`. */
+int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t key_bits, int32_t location);
+/* Exclusive scan in place (offset_scan.wgsl:22-67); *total receives the sum (host pointer). */
+int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, int32_t location);
+/* The pinned fp32 exp of the kernels, evaluated on the device (y = exp(x)). */
+int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
+
+/* ---- host utilities (no GPU needed) ----------------------------------------------------------- */
+/* Camera.getUniform() (src/renderer/camera.js:87-98) with wgpu-matrix lookAt / perspective
+ * (camera.js:135-142, 0..1 clip depth) restated: fills the 176-byte block for a camera at `eye`
+ * looking at `target`, vertical field of view fovy_deg, image width x height. */
+int gs_camera_view(const float eye[3], const float target[3], const float up[3], float fovy_deg,
+                   uint32_t width, uint32_t height, float z_near, float z_far, gs_view* out);
+
+/* Seeded synthetic scene in the packed layout (59*count floats). kind 0: one isotropic cluster
+ * N(0,1)^3; kind 1: mixture of `clusters` anisotropic clusters in a box of edge `box`. Other
+ * attributes: log-scale N(-4, 0.5^2), quaternion N(0,1)^4 normalised, opacity logit N(0, 1.5^2),
+ * DC N(0, 0.5^2), rest N(0, 0.05^2). Bit-identical on every host. */
+int gs_synth_scene(uint32_t kind, uint32_t count, uint64_t seed, uint32_t clusters, float box, float* packed);
+
+/* Perturbs a packed scene in place: means += N(0, sigma_mean^2), SH (DC and rest) += N(0, sigma_sh^2). */
+int gs_perturb_scene(float* packed, uint32_t count, uint64_t seed, float sigma_mean, float sigma_sh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WEBGS_GS_H */

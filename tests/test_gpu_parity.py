@@ -1,0 +1,127 @@
+"""GPU pipeline vs the CPU oracle: bit-exact binning (tilesTouched, meta, offsets, I, keys, values,
+tile ranges) and pixels within 1e-4 max-abs (bit-exact under the pinned fp32 semantics), through
+the C ABI (libwebgs.so)."""
+import numpy as np
+import pytest
+
+import webgs
+from webgs import workloads as W
+from helpers import assert_frame_parity, gpu_frame, oracle_frame
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ctx, packed, count, view, tile=16, factor=64, allow_overflow=False):
+    scene = ctx.upload(packed, count)
+    try:
+        g = gpu_frame(ctx, scene, view, allow_overflow=allow_overflow)
+    finally:
+        scene.close()
+    o = oracle_frame(view, packed, count, tile=tile, factor=factor)
+    return g, o
+
+
+def test_small_config_parity(gpu_ctx):
+    """The 50k-Gaussian, 512x512 configuration (seed 0)."""
+    packed = W.SMALL_SCENE.build()
+    g, o = _run(gpu_ctx, packed, W.SMALL_SCENE.count, W.SMALL_CAMERA.view())
+    assert o["instance_count"] > 100_000
+    assert_frame_parity(g, o)
+
+
+def test_cluster_scene_parity(gpu_ctx):
+    """Cluster mixture inside a box, camera inside the box (a reduced scene-scale case)."""
+    spec = W.SceneSpec(200_000, 11, 1, 64, 20.0)
+    packed = spec.build()
+    view = W.CameraSpec((0.0, 1.0, -9.0), (0.0, 0.0, 0.0), 70.0, 960, 540).view()
+    g, o = _run(gpu_ctx, packed, spec.count, view)
+    assert_frame_parity(g, o)
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (17, 17), (1000, 7), (33, 250), (640, 480)])
+def test_odd_image_sizes(gpu_ctx, w, h):
+    packed = W.SceneSpec(3000, 5, 0).build()
+    view = webgs.camera_view((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, w, h, 0.2, 100.0)
+    g, o = _run(gpu_ctx, packed, 3000, view)
+    assert_frame_parity(g, o)
+
+
+@pytest.mark.parametrize("count", [0, 1, 2, 33, 2047, 2048, 2049, 4097])
+def test_counts_across_partition_edges(gpu_ctx, count):
+    packed = W.SceneSpec(count, 7, 0).build() if count else np.zeros(0, np.float32)
+    view = webgs.camera_view((0.0, 0.0, -3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 128, 96, 0.2, 100.0)
+    g, o = _run(gpu_ctx, packed, count, view)
+    assert_frame_parity(g, o)
+
+
+@pytest.mark.parametrize("tile", [8, 16, 32])
+@pytest.mark.parametrize("digit_bits", [4, 8])
+def test_tile_and_digit_configs(tile, digit_bits):
+    packed = W.SceneSpec(20_000, 3, 0).build()
+    view = W.CameraSpec((0.0, 0.5, -4.0), (0.0, 0.0, 0.0), 60.0, 300, 200).view()
+    with webgs.Context(tile_size=tile, digit_bits=digit_bits) as ctx:
+        g, o = _run(ctx, packed, 20_000, view, tile=tile)
+    assert_frame_parity(g, o)
+
+
+@pytest.mark.parametrize("batch", [32, 64, 128, 256])
+def test_raster_batch_depths(batch):
+    packed = W.SceneSpec(20_000, 4, 0).build()
+    view = W.CameraSpec((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 60.0, 256, 256).view()
+    with webgs.Context(raster_batch=batch) as ctx:
+        g, o = _run(ctx, packed, 20_000, view)
+    assert_frame_parity(g, o)
+
+
+def test_instance_overflow_truncates_like_reference():
+    """factor 1: far more instances than slots; emit drops slots >= max_instance (emit.wgsl:57-59),
+    the call reports GS_ERR_OVERFLOW and still writes the truncated frame."""
+    packed = W.SceneSpec(5000, 8, 0).build()
+    view = W.CameraSpec((0.0, 0.0, -2.5), (0.0, 0.0, 0.0), 60.0, 256, 256).view()
+    with webgs.Context(max_instance_factor=1) as ctx:
+        g, o = _run(ctx, packed, 5000, view, factor=1, allow_overflow=True)
+        assert g.get("overflow")
+        with pytest.raises(webgs.GsError) as ei:
+            s = ctx.upload(packed, 5000)
+            try:
+                ctx.forward(s, view)
+            finally:
+                s.close()
+        assert ei.value.code == 3
+    assert o["instance_count"] > o["max_instance"] == 5000
+    assert_frame_parity(g, o)
+
+
+def test_equal_depth_ties_keep_gaussian_order(gpu_ctx):
+    """All splats on one plane facing the camera: heavy depth16 ties; ties sort by Gaussian index."""
+    n = 4000
+    packed = W.SceneSpec(n, 9, 0).build()
+    pos = packed[: 3 * n].reshape(n, 3)
+    pos[:, 2] = 0.0
+    view = W.CameraSpec((0.0, 0.0, -3.0), (0.0, 0.0, 0.0), 60.0, 200, 200).view()
+    g, o = _run(gpu_ctx, packed, n, view)
+    assert_frame_parity(g, o)
+    k, v = g["keys"], g["vals"]
+    same = k[1:] == k[:-1]
+    assert same.any() and (v[1:][same] > v[:-1][same]).all()
+
+
+def test_repeat_frames_are_deterministic(gpu_ctx):
+    packed = W.SceneSpec(30_000, 10, 0).build()
+    view = W.CameraSpec((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 60.0, 320, 240).view()
+    scene = gpu_ctx.upload(packed, 30_000)
+    try:
+        a = gpu_frame(gpu_ctx, scene, view)
+        b = gpu_frame(gpu_ctx, scene, view)
+    finally:
+        scene.close()
+    for key in ("keys", "vals", "ranges", "rgba8"):
+        np.testing.assert_array_equal(a[key], b[key])
+    np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
+
+
+def test_scene_scale_config_parity(gpu_ctx):
+    """1M Gaussians, 64-cluster mixture in a 20^3 box, 1920x1080, camera inside the box."""
+    packed = W.SCENE_1M.build()
+    g, o = _run(gpu_ctx, packed, W.SCENE_1M.count, W.CAMERA_1080P.view())
+    assert_frame_parity(g, o)

@@ -1,0 +1,72 @@
+"""Building blocks on the GPU vs the oracle: the radix sort (gs_sort_pairs), the decoupled-lookback
+scan (gs_exclusive_scan) and the pinned exp (gs_exp_f32), through the C ABI."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _stable_ref(keys, vals, key_bits):
+    mask = np.uint64((1 << key_bits) - 1)
+    order = np.argsort(keys.astype(np.uint64) & mask, kind="stable")
+    return keys[order], vals[order]
+
+
+@pytest.mark.parametrize("n", [1, 2, 255, 256, 4095, 4096, 4097, 100_003, 3_000_000])
+def test_sort_random_keys(gpu_ctx, n):
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    k, v = gpu_ctx.sort_pairs(keys, vals, 32)
+    rk, rv = _stable_ref(keys, vals, 32)
+    np.testing.assert_array_equal(k, rk)
+    np.testing.assert_array_equal(v, rv)
+
+
+def test_sort_matches_literal_reference_radix(gpu_ctx):
+    rng = np.random.default_rng(5)
+    n = 70_000
+    keys = (rng.integers(0, 300, n).astype(np.uint32) << 16) | rng.integers(0, 50, n).astype(np.uint32)
+    vals = rng.permutation(n).astype(np.uint32)
+    k, v = gpu_ctx.sort_pairs(keys, vals, 32)
+    ok, ov = oracle.radix_sort_pairs(keys, vals, 4)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(v, ov)
+
+
+def test_sort_all_equal_and_partial_bits(gpu_ctx):
+    n = 50_000
+    keys = np.full(n, 0xABCD1234, np.uint32)
+    vals = np.arange(n, dtype=np.uint32)[::-1].copy()
+    k, v = gpu_ctx.sort_pairs(keys, vals, 32)
+    np.testing.assert_array_equal(v, vals)  # stability: input order kept
+    rng = np.random.default_rng(9)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    k, v = gpu_ctx.sort_pairs(keys, np.arange(n, dtype=np.uint32), 20)
+    rk, rv = _stable_ref(keys, np.arange(n, dtype=np.uint32), 20)
+    np.testing.assert_array_equal(v, rv)
+
+
+@pytest.mark.parametrize("n", [0, 1, 7, 2048, 2049, 1_000_001])
+def test_exclusive_scan(gpu_ctx, n):
+    rng = np.random.default_rng(n)
+    data = rng.integers(0, 70, n).astype(np.uint32)
+    out, tot = gpu_ctx.exclusive_scan(data)
+    ref, rtot = oracle.exclusive_scan(data)
+    np.testing.assert_array_equal(out, ref)
+    assert tot == rtot
+
+
+def test_pinned_exp_bitwise(gpu_ctx):
+    rng = np.random.default_rng(0)
+    x = np.concatenate([
+        rng.uniform(-110, 95, 2_000_000).astype(np.float32),
+        rng.uniform(-6, 0, 2_000_000).astype(np.float32),
+        np.array([0.0, -0.0, 88.7, 88.8, 89.0, -103.9, -104.0, -104.1, np.inf, -np.inf, np.nan, 1e-30, -1e-30],
+                 np.float32),
+    ])
+    g = gpu_ctx.exp(x)
+    o = oracle.expf(x)
+    np.testing.assert_array_equal(g.view(np.uint32), o.view(np.uint32))

@@ -1,0 +1,475 @@
+// gs_binning.cu -- offset scan, emit, radix sort and tile ranges of the splat pipeline:
+//   offset scan  src/shaders/offset_scan.wgsl:22-67   -> k_scan_emit (single-pass decoupled lookback)
+//   emit         src/shaders/emit.wgsl:28-66          -> k_scan_emit (fused, load-balanced)
+//   indirect arg src/shaders/indirect_arg.wgsl:14-27  -> FrameCtl counts read on the device
+//   radix sort   src/shaders/radix_parallel.wgsl      -> k_onesweep (one kernel per digit pass)
+//   tile ranges  src/shaders/tile_ranges.wgsl:7-34    -> k_tile_ranges
+//
+// Ordering: every kernel that chains partitions takes a ticket from FrameCtl so that partition p
+// only ever waits on partitions already owned by running CTAs; every wait is bounded
+// (warp_lookback).
+#include "gs_kernels.h"
+
+namespace gs {
+namespace {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Block-wide exclusive scan of one value per thread (THREADS a multiple of 32). Returns the
+// exclusive prefix; *total receives the block sum. Uses `warp_sums` (THREADS/32 words).
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int kWarps = THREADS / 32;
+        uint32_t s = lane < (uint32_t)kWarps ? warp_sums[lane] : 0u;
+        uint32_t si = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= (uint32_t)o) si += t;
+        }
+        if (lane < (uint32_t)kWarps) warp_sums[lane] = si - s;  // exclusive warp offsets
+        if (lane == (uint32_t)kWarps - 1u) warp_sums[kWarps] = si;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + incl - v;
+    *total = warp_sums[THREADS / 32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_frame_begin(FrameCtl* ctl) {
+    const uint32_t t = threadIdx.x;
+    if (t == 0) {
+        ctl->seq = (ctl->seq & ~15u) + 16u;
+        ctl->status = 0u;
+        ctl->instance_count = 0u;
+        ctl->sorted_count = 0u;
+        ctl->visible = 0u;
+        ctl->near_pass = 0u;
+    }
+    if (t < 15) ctl->tickets[t] = 0u;
+    for (uint32_t i = t; i < 8u * 256u; i += blockDim.x) ctl->hist[i] = 0u;
+}
+
+// ---- fused offset scan + emit ---------------------------------------------------------------
+// Partition p covers entries [p*2048, p*2048+2048) of counts[0..n] (n+1 entries; counts[n] = 0).
+// 1. each thread loads 8 consecutive counts (two 16-byte loads), the block scans them;
+// 2. warp 0 publishes the partition aggregate and looks back for its exclusive prefix;
+// 3. offsets[g] are written (offsets[n] = I), the partition holding entry n publishes I and
+//    min(I, max_instance) to FrameCtl (indirect_arg.wgsl:14-27);
+// 4. the partition's instances [excl, excl + total) are emitted by all 256 threads in slot order,
+//    each slot finding its Gaussian by binary search over the partition's local offsets, so one
+//    large splat never serialises a warp; keys are ((ty*tilesPerRow + tx) << 16) | depth16 in
+//    row-major tile order (emit.wgsl:55-66) and slots >= max_instance are dropped (:57-59);
+// 5. the digit histograms of every sort pass are accumulated on the fly.
+__global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __restrict__ counts,
+                                                            const uint4* __restrict__ meta, uint32_t n,
+                                                            uint32_t tiles_x, uint32_t max_instance,
+                                                            uint32_t digit_bits, uint32_t passes,
+                                                            uint32_t* __restrict__ offsets, uint32_t* __restrict__ keys,
+                                                            uint32_t* __restrict__ vals, FrameCtl* ctl,
+                                                            uint64_t* flags, uint32_t slot) {
+    __shared__ uint32_t s_off[kScanPartition + 1];
+    __shared__ uint2 s_meta[kScanPartition];  // (min, max) packed rects
+    __shared__ uint32_t s_depth[kScanPartition];
+    __shared__ uint32_t s_hist[8 * 256];
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    __shared__ uint32_t s_part, s_excl, s_seq;
+
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        s_part = atomicAdd(&ctl->tickets[slot], 1u);
+        s_seq = ctl->seq + slot;
+    }
+    const uint32_t radix = 1u << digit_bits;
+    for (uint32_t i = tid; i < passes * radix; i += kScanThreads) s_hist[i] = 0u;
+    __syncthreads();
+    const uint32_t part = s_part, seq = s_seq;
+    const uint32_t entries = n + 1u;
+    const uint32_t base = part * kScanPartition;
+    const uint32_t g0 = base + tid * kScanItems;
+
+    uint32_t c[kScanItems];
+    if (g0 + kScanItems <= entries) {
+        const uint4 a = *reinterpret_cast<const uint4*>(counts + g0);
+        const uint4 b = *reinterpret_cast<const uint4*>(counts + g0 + 4);
+        c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w; c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+    } else {
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) c[k] = (g0 + k < entries) ? counts[g0 + k] : 0u;
+    }
+    uint32_t tsum = 0, vis = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        tsum += c[k];
+        vis += c[k] != 0u ? 1u : 0u;
+    }
+    uint32_t total;
+    const uint32_t texcl = block_exclusive_scan<kScanThreads>(tsum, s_warp, &total);
+
+    // publish the aggregate, then look back for the exclusive prefix
+    if (tid < 32) {
+        if (tid == 0) st_relaxed_u64(flags + part, make_word(seq, part == 0 ? kFlagInclusive : kFlagAggregate, total));
+        const uint32_t excl = warp_lookback(flags, part, seq, &ctl->status);
+        if (tid == 0) {
+            if (part != 0) st_relaxed_u64(flags + part, make_word(seq, kFlagInclusive, excl + total));
+            s_excl = excl;
+        }
+    }
+    // local offsets and rects into shared memory
+    {
+        uint32_t run = texcl;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t lg = tid * kScanItems + k;
+            s_off[lg] = run;
+            if (c[k] != 0u) {
+                const uint4 m = meta[g0 + k];
+                s_meta[lg] = make_uint2(m.x, m.y);
+                s_depth[lg] = m.z & 0xFFFFu;
+            }
+            run += c[k];
+        }
+        if (tid == 0) s_off[kScanPartition] = total;
+    }
+    if (vis) atomicAdd(&ctl->visible, vis);
+    __syncthreads();
+    const uint32_t excl = s_excl;
+
+    // offsets (the debug view of offset_scan.wgsl's in-place result)
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        const uint32_t g = g0 + k;
+        if (g < entries) offsets[g] = excl + s_off[tid * kScanItems + k];
+        if (g == n) {
+            const uint32_t I = excl + s_off[tid * kScanItems + k];
+            ctl->instance_count = I;
+            ctl->sorted_count = I < max_instance ? I : max_instance;
+            if (I > max_instance) atomicOr(&ctl->status, kDevOverflow);
+        }
+    }
+
+    // emit
+    const uint32_t mask = radix - 1u;
+    for (uint32_t i = tid; i < total; i += kScanThreads) {
+        const uint32_t slot_i = excl + i;
+        if (slot_i >= max_instance) break;
+        // largest lg with s_off[lg] <= i (counts of that Gaussian > 0 since s_off[lg+1] > i)
+        uint32_t lo = 0, hi = kScanPartition;  // invariant: s_off[lo] <= i < s_off[hi]
+        while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_off[mid] <= i) lo = mid; else hi = mid;
+        }
+        const uint32_t k = i - s_off[lo];
+        const uint2 m = s_meta[lo];
+        const uint32_t minX = m.x & 0xFFFFu, minY = m.x >> 16u, maxX = m.y & 0xFFFFu;
+        const uint32_t w = maxX - minX + 1u;
+        const uint32_t ty = minY + k / w, tx = minX + k % w;
+        const uint32_t key = ((ty * tiles_x + tx) << 16u) | s_depth[lo];
+        keys[slot_i] = key;
+        vals[slot_i] = base + lo;
+        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < passes * radix; i += kScanThreads)
+        if (s_hist[i]) atomicAdd(&ctl->hist[i], s_hist[i]);
+}
+
+// ---- standalone exclusive scan (offset_scan.wgsl:22-67 semantics, any n) ------------------------
+__global__ void __launch_bounds__(kScanThreads) k_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_out,
+                                                                 FrameCtl* ctl, uint64_t* flags, uint32_t slot) {
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    __shared__ uint32_t s_part, s_excl, s_seq;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        s_part = atomicAdd(&ctl->tickets[slot], 1u);
+        s_seq = ctl->seq + slot;
+    }
+    __syncthreads();
+    const uint32_t part = s_part, seq = s_seq;
+    const uint32_t g0 = part * kScanPartition + tid * kScanItems;
+    uint32_t c[kScanItems], tsum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        c[k] = (g0 + k < n) ? data[g0 + k] : 0u;
+        tsum += c[k];
+    }
+    uint32_t total;
+    const uint32_t texcl = block_exclusive_scan<kScanThreads>(tsum, s_warp, &total);
+    if (tid < 32) {
+        if (tid == 0) st_relaxed_u64(flags + part, make_word(seq, part == 0 ? kFlagInclusive : kFlagAggregate, total));
+        const uint32_t excl = warp_lookback(flags, part, seq, &ctl->status);
+        if (tid == 0) {
+            if (part != 0) st_relaxed_u64(flags + part, make_word(seq, kFlagInclusive, excl + total));
+            s_excl = excl;
+        }
+    }
+    __syncthreads();
+    uint32_t run = s_excl + texcl;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        if (g0 + k < n) data[g0 + k] = run;
+        run += c[k];
+    }
+    if (part == gridDim.x - 1u && tid == kScanThreads - 1u) *total_out = run;
+}
+
+// ---- digit histograms for a standalone sort ---------------------------------------------------
+__global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint32_t digit_bits, uint32_t passes,
+                             uint32_t* hist) {
+    __shared__ uint32_t s_hist[8 * 256];
+    const uint32_t radix = 1u << digit_bits, mask = radix - 1u;
+    for (uint32_t i = threadIdx.x; i < passes * radix; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < passes * radix; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+// ---- onesweep radix pass ------------------------------------------------------------------------
+// One stable counting-sort pass on digit (key >> shift) & (RADIX-1) (radix_parallel.wgsl:26-160 in
+// one kernel). Persistent CTAs take partitions of 4096 keys by ticket. Per partition:
+//   - keys load warp-striped (item k of lane l of warp w is element w*512 + k*32 + l), so every
+//     load is a 128-byte line and the warp processes its elements in index order;
+//   - __match_any_sync groups the lanes holding the same digit; a lane's rank is the count of
+//     equal digits in earlier items of its warp plus its rank among the equal lanes (stable);
+//   - per-digit warp counts are scanned across warps (warp order = index order), the CTA's digit
+//     totals are published as lookback aggregates and the inclusive prefix of every digit is found
+//     by decoupled lookback (one thread per digit);
+//   - keys/values are staged in shared memory in local sorted order and written out at
+//     global_digit_base + rank, which keeps runs of equal digits contiguous in global memory.
+template <int BITS>
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __restrict__ keys_in,
+                                                           const uint32_t* __restrict__ vals_in,
+                                                           uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                           const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
+                                                           const uint32_t* __restrict__ hist, FrameCtl* ctl,
+                                                           uint64_t* flags, uint32_t slot) {
+    constexpr uint32_t RADIX = 1u << BITS;
+    constexpr uint32_t MASK = RADIX - 1u;
+    constexpr uint32_t WARPS = kSortThreads / 32;
+    constexpr uint32_t PER_WARP = kSortItems * 32;
+    __shared__ uint32_t s_keys[kSortPartition];
+    __shared__ uint32_t s_vals[kSortPartition];
+    __shared__ uint32_t s_whist[WARPS][RADIX];
+    __shared__ uint32_t s_gbase[RADIX];     // global exclusive digit base of this pass
+    __shared__ uint32_t s_dstart[RADIX];    // local sorted start of each digit
+    __shared__ uint32_t s_out[RADIX];       // global position of local element 0 of each digit
+    __shared__ uint32_t s_warp[WARPS + 1];
+    __shared__ uint32_t s_part, s_seq;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t n = n_dev ? *n_dev : n_host;
+    const uint32_t nparts = (n + kSortPartition - 1u) / kSortPartition;
+
+    // global digit bases of this pass: exclusive scan of the histogram
+    {
+        const uint32_t h = tid < RADIX ? hist[tid] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan<kSortThreads>(h, s_warp, &tot);
+        if (tid < RADIX) s_gbase[tid] = ex;
+    }
+    if (tid == 0) s_seq = ctl->seq + slot;
+
+    while (true) {
+        __syncthreads();
+        if (tid == 0) s_part = atomicAdd(&ctl->tickets[slot], 1u);
+        __syncthreads();
+        const uint32_t part = s_part, seq = s_seq;
+        if (part >= nparts) break;
+        const uint32_t base = part * kSortPartition;
+        const uint32_t valid_n = min(kSortPartition, n - base);
+
+        for (uint32_t d = lane; d < RADIX; d += 32) s_whist[warp][d] = 0u;
+        __syncwarp();
+
+        uint32_t key[kSortItems], val[kSortItems];
+        uint16_t rank[kSortItems];
+        const uint32_t wbase = base + warp * PER_WARP;
+#pragma unroll
+        for (uint32_t k = 0; k < kSortItems; ++k) {
+            const uint32_t idx = wbase + k * 32u + lane;
+            const bool ok = idx < n;
+            key[k] = ok ? keys_in[idx] : 0xFFFFFFFFu;
+            val[k] = ok ? vals_in[idx] : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kSortItems; ++k) {
+            const uint32_t idx = wbase + k * 32u + lane;
+            const bool ok = idx < n;
+            const uint32_t d = ok ? ((key[k] >> shift) & MASK) : RADIX;  // RADIX marks padding
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t pre = ok ? s_whist[warp][d] : 0u;
+            __syncwarp();
+            if (ok) {
+                const uint32_t below = peers & ((1u << lane) - 1u);
+                if (below == 0u) s_whist[warp][d] = pre + __popc(peers);
+                rank[k] = (uint16_t)(pre + __popc(below));
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+
+        // per digit: exclusive over warps, CTA total, lookback
+        uint32_t cta_total = 0;
+        if (tid < RADIX) {
+#pragma unroll
+            for (uint32_t w = 0; w < WARPS; ++w) {
+                const uint32_t c = s_whist[w][tid];
+                s_whist[w][tid] = cta_total;
+                cta_total += c;
+            }
+            st_relaxed_u64(flags + (size_t)part * RADIX + tid,
+                           make_word(seq, part == 0 ? kFlagInclusive : kFlagAggregate, cta_total));
+        }
+        uint32_t dtot;
+        const uint32_t dstart = block_exclusive_scan<kSortThreads>(tid < RADIX ? cta_total : 0u, s_warp, &dtot);
+        if (tid < RADIX) {
+            s_dstart[tid] = dstart;
+            // serial lookback per digit (one thread per digit, bounded waits)
+            uint32_t excl = 0;
+            if (part != 0) {
+                int64_t j = (int64_t)part - 1;
+                const uint32_t want = seq & kSeqMask;
+                while (j >= 0) {
+                    const uint64_t* p = flags + (size_t)j * RADIX + tid;
+                    uint64_t w = ld_relaxed_u64(p);
+                    uint32_t spins = 0;
+                    while (word_seq(w) != want || word_flag(w) == 0u) {
+                        if (++spins > kSpinLimit) {
+                            atomicOr(&ctl->status, kDevTimeout);
+                            w = make_word(want, kFlagInclusive, 0u);
+                            break;
+                        }
+                        if (spins > 64u) __nanosleep(64);
+                        w = ld_relaxed_u64(p);
+                    }
+                    excl += word_value(w);
+                    if (word_flag(w) == kFlagInclusive) break;
+                    --j;
+                }
+                st_relaxed_u64(flags + (size_t)part * RADIX + tid, make_word(seq, kFlagInclusive, excl + cta_total));
+            }
+            s_out[tid] = s_gbase[tid] + excl - dstart;
+        }
+        __syncthreads();
+
+        // local sorted order in shared memory
+#pragma unroll
+        for (uint32_t k = 0; k < kSortItems; ++k) {
+            const uint32_t idx = wbase + k * 32u + lane;
+            if (idx < n) {
+                const uint32_t d = (key[k] >> shift) & MASK;
+                const uint32_t pos = s_dstart[d] + s_whist[warp][d] + rank[k];
+                s_keys[pos] = key[k];
+                s_vals[pos] = val[k];
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < valid_n; i += kSortThreads) {
+            const uint32_t k = s_keys[i];
+            const uint32_t gpos = s_out[(k >> shift) & MASK] + i;
+            if (gpos < n) {  // always true unless a lookback timed out (status already set)
+                keys_out[gpos] = k;
+                vals_out[gpos] = s_vals[i];
+            }
+        }
+    }
+}
+
+// ---- tile ranges (tile_ranges.wgsl:7-34) over the sorted prefix -----------------------------------
+// Tiles outside [0, tiles) can only come from a timed-out sort; they are skipped.
+__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCtl* ctl, uint32_t tiles,
+                              uint32_t* __restrict__ ranges) {
+    const uint32_t n = ctl->sorted_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t tile = keys[i] >> 16u;
+        if (tile >= tiles) continue;
+        if (i == 0u) {
+            ranges[tile * 2u] = 0u;
+        } else {
+            const uint32_t prev = keys[i - 1u] >> 16u;
+            if (tile > prev && prev < tiles) {
+                ranges[prev * 2u + 1u] = i;
+                ranges[tile * 2u] = i;
+            }
+        }
+        if (i == n - 1u) ranges[tile * 2u + 1u] = n;
+    }
+}
+
+int sm_count() {
+    static int cached = 0;
+    if (cached == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached = v > 0 ? v : 1;
+    }
+    return cached;
+}
+
+}  // namespace
+
+void launch_frame_begin(FrameCtl* ctl, cudaStream_t s) { k_frame_begin<<<1, 256, 0, s>>>(ctl); }
+
+void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uint32_t tiles_x, uint32_t max_instance,
+                      uint32_t digit_bits, uint32_t passes, uint32_t* offsets, uint32_t* keys, uint32_t* vals,
+                      FrameCtl* ctl, uint64_t* flags, uint32_t slot, cudaStream_t s) {
+    const uint32_t parts = (n + 1u + kScanPartition - 1u) / kScanPartition;
+    k_scan_emit<<<parts, kScanThreads, 0, s>>>(counts, meta, n, tiles_x, max_instance, digit_bits, passes, offsets,
+                                               keys, vals, ctl, flags, slot);
+}
+
+void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
+                           uint32_t slot, cudaStream_t s) {
+    const uint32_t parts = n == 0 ? 1u : (n + kScanPartition - 1u) / kScanPartition;
+    k_exclusive_scan<<<parts, kScanThreads, 0, s>>>(data, n, total_dev, ctl, flags, slot);
+}
+
+void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t passes, uint32_t* hist,
+                       cudaStream_t s) {
+    uint32_t blocks = (n + 1023u) / 1024u;
+    const uint32_t cap = (uint32_t)sm_count() * 4u;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    k_digit_hist<<<blocks, 256, 0, s>>>(keys, n, digit_bits, passes, hist);
+}
+
+void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                     uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
+                     const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot, int grid_cap,
+                     cudaStream_t s) {
+    uint32_t parts = (max_n + kSortPartition - 1u) / kSortPartition;
+    const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
+    if (parts > cap) parts = cap;
+    if (parts == 0) parts = 1;
+    if (digit_bits == 4)
+        k_onesweep<4><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, hist,
+                                                     ctl, flags, slot);
+    else
+        k_onesweep<8><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, hist,
+                                                     ctl, flags, slot);
+}
+
+void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,
+                        cudaStream_t s) {
+    const uint32_t grid = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
+    k_tile_ranges<<<grid, 256, 0, s>>>(keys, ctl, tiles, ranges);
+}
+
+}  // namespace gs

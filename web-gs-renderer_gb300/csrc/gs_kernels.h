@@ -1,0 +1,67 @@
+// gs_kernels.h -- launch wrappers of the splat kernels (host side), used by the C ABI in gs_api.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gs_common.cuh"
+
+namespace gs {
+
+// Per-Gaussian raster record written by preprocess (three float4 per Gaussian):
+//   r0 = (pixel.x, pixel.y, conic.x, conic.y)
+//   r1 = (conic.z, opacity, color.r, color.g)
+//   r2 = (color.b, power cut-off below which alpha < 1/255 for sure, 0, 0)
+constexpr int kRecFloat4 = 3;
+
+// ---- scene layout -------------------------------------------------------------------------
+// packed (reference layout, preprocess.wgsl:16-24) -> rows of the structure-of-arrays layout.
+void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s);
+// rows -> packed (used for gradients).
+void launch_rows_to_pack(const float* rows, uint32_t n, uint32_t stride, float* packed, cudaStream_t s);
+
+// ---- frame ----------------------------------------------------------------------------------
+void launch_frame_begin(FrameCtl* ctl, cudaStream_t s);
+
+void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
+                       float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s);
+
+// Offset scan (decoupled lookback) fused with emit and the sort's digit histograms.
+constexpr uint32_t kScanItems = 8;
+constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanPartition = kScanItems * kScanThreads;
+void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uint32_t tiles_x, uint32_t max_instance,
+                      uint32_t digit_bits, uint32_t passes, uint32_t* offsets, uint32_t* keys, uint32_t* vals,
+                      FrameCtl* ctl, uint64_t* flags, uint32_t slot, cudaStream_t s);
+
+// Onesweep LSD radix pass. n comes from *n_dev when non-null, else n_host.
+constexpr uint32_t kSortThreads = 256;
+constexpr uint32_t kSortItems = 16;
+constexpr uint32_t kSortPartition = kSortThreads * kSortItems;
+void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                     uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
+                     const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot, int grid_cap,
+                     cudaStream_t s);
+// Digit histograms of all passes for a standalone sort.
+void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t passes, uint32_t* hist,
+                       cudaStream_t s);
+// Standalone exclusive scan (decoupled lookback); total written to *total_dev.
+void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
+                           uint32_t slot, cudaStream_t s);
+
+void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,
+                        cudaStream_t s);
+
+struct RasterOut {
+    uint32_t* rgba8;     // W*H packed rgba8 or null
+    float* rgb;          // W*H*3 or null
+    float* final_t;      // W*H or null
+    uint32_t* n_contrib; // W*H or null
+};
+// ctl (optional) bounds every range by the sorted count; n bounds the Gaussian indices.
+void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec,
+                   uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x,
+                   uint32_t tiles_y, const RasterOut& out, cudaStream_t s);
+
+void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
+
+}  // namespace gs

@@ -1,0 +1,309 @@
+// gs_preprocess.cu -- per-Gaussian preprocess (src/shaders/preprocess.wgsl:58-284) and the scene
+// layout conversions.
+//
+// One thread per Gaussian over the structure-of-arrays scene rows: every attribute load of a warp
+// is one 128-byte coalesced line, so the kernel streams the 236 bytes of a visible Gaussian at HBM
+// rate. The arithmetic follows the WGSL source order with no contraction (the file is built with
+// -fmad=false) so that every output bit equals the reference restatement.
+#include "gs_kernels.h"
+
+namespace gs {
+namespace {
+
+struct M3 { float m[3][3]; };  // column-major, m[col][row] as WGSL mat3x3f
+
+__device__ __forceinline__ M3 mul33(const M3& a, const M3& b) {
+    M3 c;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            float s = a.m[0][i] * b.m[j][0];
+            s = s + a.m[1][i] * b.m[j][1];
+            s = s + a.m[2][i] * b.m[j][2];
+            c.m[j][i] = s;
+        }
+    return c;
+}
+__device__ __forceinline__ M3 tr33(const M3& a) {
+    M3 t;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) t.m[j][i] = a.m[i][j];
+    return t;
+}
+
+__global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
+                                                    const ViewBlock* __restrict__ vb, uint32_t tile,
+                                                    float4* __restrict__ rec, uint4* __restrict__ meta,
+                                                    uint32_t* __restrict__ counts, FrameCtl* ctl) {
+    __shared__ ViewBlock sv;
+    if (threadIdx.x < 44) reinterpret_cast<uint32_t*>(&sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(vb)[threadIdx.x];
+    __syncthreads();
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g == 0) counts[n] = 0u;  // the N+1-th scan entry (cleared by renderer.js:826)
+    const uint32_t gg = g < n ? g : 0u;  // out-of-range threads compute on entry 0, write nothing
+    const float px = __ldg(rows + (size_t)(kRowPos + 0) * stride + gg);
+    const float py = __ldg(rows + (size_t)(kRowPos + 1) * stride + gg);
+    const float pz = __ldg(rows + (size_t)(kRowPos + 2) * stride + gg);
+
+    // uniforms.view * vec4f(position, 1.0f)  (:79)
+    float pv[4], clip[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float s = sv.view[0 * 4 + i] * px;
+        s = s + sv.view[1 * 4 + i] * py;
+        s = s + sv.view[2 * 4 + i] * pz;
+        s = s + sv.view[3 * 4 + i] * 1.0f;
+        pv[i] = s;
+    }
+    // near culling (:83); the block counts its survivors for the frame statistics
+    const bool near_ok = g < n && !(pv[2] >= -kZNearView);
+    const int block_near = __syncthreads_count(near_ok);
+    if (threadIdx.x == 0 && block_near) atomicAdd(&ctl->near_pass, (uint32_t)block_near);
+    if (g >= n) return;
+    if (!near_ok) {
+        counts[g] = 0u;
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float s = sv.viewProj[0 * 4 + i] * px;
+        s = s + sv.viewProj[1 * 4 + i] * py;
+        s = s + sv.viewProj[2 * 4 + i] * pz;
+        s = s + sv.viewProj[3 * 4 + i] * 1.0f;
+        clip[i] = s;
+    }
+    const float W = sv.textureSize[0], H = sv.textureSize[1];
+    const float wden = clip[3] + kSmallValue;
+    const float ndcx = clip[0] / wden, ndcy = clip[1] / wden, ndcz = clip[2] / wden;
+    const float pixx = ((ndcx + 1.0f) * W - 1.0f) * 0.5f;
+    const float pixy = ((ndcy + 1.0f) * H - 1.0f) * 0.5f;
+
+    // 3D covariance (:95-100): R * S * transpose(S) * transpose(R)
+    const float sx = pinned_expf(__ldg(rows + (size_t)(kRowScale + 0) * stride + g));
+    const float sy = pinned_expf(__ldg(rows + (size_t)(kRowScale + 1) * stride + g));
+    const float sz = pinned_expf(__ldg(rows + (size_t)(kRowScale + 2) * stride + g));
+    const float q0 = __ldg(rows + (size_t)(kRowQuat + 0) * stride + g);
+    const float q1 = __ldg(rows + (size_t)(kRowQuat + 1) * stride + g);
+    const float q2 = __ldg(rows + (size_t)(kRowQuat + 2) * stride + g);
+    const float q3 = __ldg(rows + (size_t)(kRowQuat + 3) * stride + g);
+    const float qlen = sqrtf(((q1 * q1 + q2 * q2) + q3 * q3) + q0 * q0);
+    const float qx = q1 / qlen, qy = q2 / qlen, qz = q3 / qlen, qw = q0 / qlen;
+    const float x2 = qx + qx, y2 = qy + qy, z2 = qz + qz;
+    const float xx = qx * x2, xy = qx * y2, xz = qx * z2;
+    const float yy = qy * y2, yz = qy * z2, zz = qz * z2;
+    const float wx = qw * x2, wy = qw * y2, wz = qw * z2;
+    M3 R;
+    R.m[0][0] = 1.0f - (yy + zz); R.m[0][1] = xy + wz;          R.m[0][2] = xz - wy;
+    R.m[1][0] = xy - wz;          R.m[1][1] = 1.0f - (xx + zz); R.m[1][2] = yz + wx;
+    R.m[2][0] = xz + wy;          R.m[2][1] = yz - wx;          R.m[2][2] = 1.0f - (xx + yy);
+    M3 S;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) S.m[j][i] = 0.0f;
+    S.m[0][0] = sx; S.m[1][1] = sy; S.m[2][2] = sz;
+    const M3 cov = mul33(mul33(mul33(R, S), tr33(S)), tr33(R));
+
+    // calculateCovariance2D (:251-269)
+    const float limx = kFrustumExtended * sv.tanFov[0];
+    const float limy = kFrustumExtended * sv.tanFov[1];
+    const float tz = pv[2];
+    const float tx = fminf(limx, fmaxf(-limx, pv[0] / tz)) * tz;
+    const float ty = fminf(limy, fmaxf(-limy, pv[1] / tz)) * tz;
+    const float fx = sv.focal[0], fy = sv.focal[1];
+    // J: mat3x2 columns (fx/z, 0), (0, fy/z), (-fx*x/z^2, -fy*y/z^2)
+    float J[3][2];
+    J[0][0] = fx / tz; J[0][1] = 0.0f;
+    J[1][0] = 0.0f;    J[1][1] = fy / tz;
+    J[2][0] = (-fx * tx) / (tz * tz);
+    J[2][1] = (-fy * ty) / (tz * tz);
+    M3 Wm;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) Wm.m[c][r] = sv.view[c * 4 + r];
+    const M3 Wt = tr33(Wm);
+    float A[3][2], B[3][2];
+    // J * W
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            float s = J[0][i] * Wm.m[j][0];
+            s = s + J[1][i] * Wm.m[j][1];
+            s = s + J[2][i] * Wm.m[j][2];
+            A[j][i] = s;
+        }
+    // * covariance
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            float s = A[0][i] * cov.m[j][0];
+            s = s + A[1][i] * cov.m[j][1];
+            s = s + A[2][i] * cov.m[j][2];
+            B[j][i] = s;
+        }
+    // * transpose(W)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            float s = B[0][i] * Wt.m[j][0];
+            s = s + B[1][i] * Wt.m[j][1];
+            s = s + B[2][i] * Wt.m[j][2];
+            A[j][i] = s;
+        }
+    // * transpose(J)
+    float C[2][2];
+#pragma unroll
+    for (int col = 0; col < 2; ++col)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            float s = A[0][i] * J[0][col];
+            s = s + A[1][i] * J[1][col];
+            s = s + A[2][i] * J[2][col];
+            C[col][i] = s;
+        }
+    const float ca = C[0][0] + 0.3f, cb = C[0][1], cc = C[1][1] + 0.3f;
+
+    // det, calculateRadius (:103-104, :271-275)
+    const float det = ca * cc - cb * cb;
+    const float mid = 0.5f * (ca + cc);
+    const float lambda = mid + sqrtf(fmaxf(0.1f, mid * mid - det));
+    const float radius = ceilf(3.0f * sqrtf(lambda));
+
+    // conic and sigmoid opacity (:106-112, :203-205)
+    const float op_logit = __ldg(rows + (size_t)kRowOpacity * stride + g);
+    const float opacity = 1.0f / (1.0f + pinned_expf(-op_logit));
+    const float conx = cc / det, cony = -cb / det, conz = ca / det;
+
+    // view direction and degree-3 SH colour (:114-115, :219-249)
+    const float dx = px - sv.cameraPos[0], dy = py - sv.cameraPos[1], dz = pz - sv.cameraPos[2];
+    const float dlen = sqrtf((dx * dx + dy * dy) + dz * dz);
+    const float x = dx / dlen, y = dy / dlen, z = dz / dlen;
+    const float sxx = x * x, syy = y * y, szz = z * z;
+    const float sxy = x * y, syz = y * z, sxz = x * z;
+    float w[16];
+    w[1] = kShC1 * y;
+    w[2] = kShC1 * z;
+    w[3] = kShC1 * x;
+    w[4] = kShC2_0 * sxy;
+    w[5] = kShC2_1 * syz;
+    w[6] = kShC2_2 * ((2.0f * szz - sxx) - syy);
+    w[7] = kShC2_3 * sxz;
+    w[8] = kShC2_4 * (sxx - syy);
+    w[9] = (kShC3_0 * y) * (3.0f * sxx - syy);
+    w[10] = (kShC3_1 * sxy) * z;
+    w[11] = (kShC3_2 * y) * ((4.0f * szz - sxx) - syy);
+    w[12] = (kShC3_3 * z) * ((2.0f * szz - 3.0f * sxx) - 3.0f * syy);
+    w[13] = (kShC3_4 * x) * ((4.0f * szz - sxx) - syy);
+    w[14] = (kShC3_5 * z) * (sxx - syy);
+    w[15] = (kShC3_6 * x) * (sxx - 3.0f * syy);
+    float col[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float* rest = rows + (size_t)(kRowRest + 15 * ch) * stride + g;
+        float r = kShC0 * __ldg(rows + (size_t)(kRowDc + ch) * stride + g);
+        r = r - w[1] * __ldg(rest + 0 * (size_t)stride);
+        r = r + w[2] * __ldg(rest + 1 * (size_t)stride);
+        r = r - w[3] * __ldg(rest + 2 * (size_t)stride);
+#pragma unroll
+        for (int k = 3; k < 15; ++k) r = r + w[k + 1] * __ldg(rest + k * (size_t)stride);
+        r = r + 0.5f;
+        col[ch] = fmaxf(r, 0.0f);
+    }
+    // power below which o * exp(power) < 1/255 for certain: ln(eps / o) less a margin far above the
+    // combined rounding error of the exp, the product and logf (see raster).
+    const float cut = logf(kEpsilon / opacity) - 1.0e-3f;
+    rec[(size_t)kRecFloat4 * g + 0] = make_float4(pixx, pixy, conx, cony);
+    rec[(size_t)kRecFloat4 * g + 1] = make_float4(conz, opacity, col[0], col[1]);
+    rec[(size_t)kRecFloat4 * g + 2] = make_float4(col[2], cut, 0.0f, 0.0f);
+
+    // frustum culling (:117-120)
+    if (pixx + radius < 0.0f || pixx - radius > W || pixy + radius < 0.0f || pixy - radius > H) {
+        counts[g] = 0u;
+        return;
+    }
+    // tile AABB, depth16, tilesTouched (:122-143)
+    const float bminx = pixx - radius, bminy = pixy - radius;
+    const float bmaxx = pixx + radius, bmaxy = pixy + radius;
+    const uint32_t tilesPerRow = ((uint32_t)W + tile - 1u) / tile;
+    const uint32_t tilesPerColumn = ((uint32_t)H + tile - 1u) / tile;
+    const float ft = (float)tile;
+    const float hx = (float)(tilesPerRow - 1u), hy = (float)(tilesPerColumn - 1u);
+    const uint32_t minTileX = (uint32_t)fminf(fmaxf(floorf(bminx / ft), 0.0f), hx);
+    const uint32_t minTileY = (uint32_t)fminf(fmaxf(floorf(bminy / ft), 0.0f), hy);
+    const uint32_t maxTileX = (uint32_t)fminf(fmaxf(floorf(bmaxx / ft), 0.0f), hx);
+    const uint32_t maxTileY = (uint32_t)fminf(fmaxf(floorf(bmaxy / ft), 0.0f), hy);
+    const uint32_t depthU16 = (uint32_t)(fminf(fmaxf(ndcz, 0.0f), 1.0f) * 65535.0f);
+    counts[g] = (maxTileX - minTileX + 1u) * (maxTileY - minTileY + 1u);
+    meta[g] = make_uint4((minTileY << 16u) | minTileX, (maxTileY << 16u) | maxTileX, depthU16, 0u);
+}
+
+// packed[block][g*width + c] -> rows[row][g]; one thread per (row, Gaussian).
+__global__ void k_pack_to_rows(const float* __restrict__ packed, uint32_t n, uint32_t stride, float* __restrict__ rows) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t r = blockIdx.y;
+    if (g >= stride) return;
+    float v = 0.0f;
+    if (g < n) {
+        uint64_t base, width, c;
+        if (r < 3) { base = 0; width = 3; c = r; }
+        else if (r < 6) { base = 3ull * n; width = 3; c = r - 3; }
+        else if (r < 10) { base = 6ull * n; width = 4; c = r - 6; }
+        else if (r < 13) { base = 10ull * n; width = 3; c = r - 10; }
+        else if (r < 14) { base = 13ull * n; width = 1; c = 0; }
+        else { base = 14ull * n; width = 45; c = r - 14; }
+        v = packed[base + (uint64_t)g * width + c];
+    }
+    rows[(size_t)r * stride + g] = v;
+}
+
+__global__ void k_rows_to_pack(const float* __restrict__ rows, uint32_t n, uint32_t stride, float* __restrict__ packed) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t r = blockIdx.y;
+    if (g >= n) return;
+    uint64_t base, width, c;
+    if (r < 3) { base = 0; width = 3; c = r; }
+    else if (r < 6) { base = 3ull * n; width = 3; c = r - 3; }
+    else if (r < 10) { base = 6ull * n; width = 4; c = r - 6; }
+    else if (r < 13) { base = 10ull * n; width = 3; c = r - 10; }
+    else if (r < 14) { base = 13ull * n; width = 1; c = 0; }
+    else { base = 14ull * n; width = 45; c = r - 14; }
+    packed[base + (uint64_t)g * width + c] = rows[(size_t)r * stride + g];
+}
+
+__global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = pinned_expf(x[i]);
+}
+
+}  // namespace
+
+void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
+                       float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s) {
+    const uint32_t blocks = (n + 255u) / 256u;
+    k_preprocess<<<blocks > 0 ? blocks : 1u, 256, 0, s>>>(rows, stride, n, view, tile, rec, meta, counts, ctl);
+}
+
+void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
+    dim3 grid((stride + 255u) / 256u, kRows);
+    k_pack_to_rows<<<grid, 256, 0, s>>>(packed, n, stride, rows);
+}
+
+void launch_rows_to_pack(const float* rows, uint32_t n, uint32_t stride, float* packed, cudaStream_t s) {
+    if (n == 0) return;
+    dim3 grid((n + 255u) / 256u, kRows);
+    k_rows_to_pack<<<grid, 256, 0, s>>>(rows, n, stride, packed);
+}
+
+void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s) {
+    if (n == 0) return;
+    k_exp<<<(n + 255u) / 256u, 256, 0, s>>>(x, y, n);
+}
+
+}  // namespace gs
