@@ -199,8 +199,8 @@ void enqueue_frame(gs_ctx* ctx, const FrameArgs& a, bool profile) {
     int cur = 0;
     for (uint32_t p = 0; p < a.passes; ++p) {
         launch_onesweep(bits, ctx->keys[cur].p, ctx->vals[cur].p, ctx->keys[cur ^ 1].p, ctx->vals[cur ^ 1].p,
-                        &ctl->sorted_count, 0, a.max_instance, p * bits, ctl->hist + p * radix, ctl, ctx->flags.p,
-                        1 + p, 0, s);
+                        &ctl->sorted_count, 0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl,
+                        ctx->flags.p, 1 + p, 0, s);
         cur ^= 1;
     }
     ctx->sorted_buf = cur;
@@ -586,12 +586,14 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
     GS_CK(cudaMemcpyAsync(v0, vals, (size_t)n * 4, kin, ctx->stream));
     FrameCtl* ctl = ctx->aux_ctl.p;
     launch_frame_begin(ctl, ctx->stream);
-    launch_digit_hist(k0, n, bits, passes, ctl->hist, ctx->stream);
+    launch_digit_hist(k0, n, bits, key_bits, ctl->hist, ctx->stream);
     uint32_t* kb[2] = {k0, k1};
     uint32_t* vb[2] = {v0, v1};
     int cur = 0;
     for (uint32_t p = 0; p < passes; ++p) {
-        launch_onesweep(bits, kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], nullptr, n, n, p * bits,
+        const uint32_t left = key_bits - p * bits;
+        const uint32_t dmask = left >= bits ? radix - 1u : (1u << left) - 1u;
+        launch_onesweep(bits, kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], nullptr, n, n, p * bits, dmask,
                         ctl->hist + p * radix, ctl, ctx->aux_flags.p, 1 + p, 0, ctx->stream);
         cur ^= 1;
     }

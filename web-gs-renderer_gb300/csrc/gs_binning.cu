@@ -225,15 +225,21 @@ __global__ void __launch_bounds__(kScanThreads) k_exclusive_scan(uint32_t* data,
 }
 
 // ---- digit histograms for a standalone sort ---------------------------------------------------
-__global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint32_t digit_bits, uint32_t passes,
+// Only the low key_bits bits take part: the last pass's digit is masked to the bits left.
+__global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits,
                              uint32_t* hist) {
     __shared__ uint32_t s_hist[8 * 256];
-    const uint32_t radix = 1u << digit_bits, mask = radix - 1u;
+    const uint32_t radix = 1u << digit_bits;
+    const uint32_t passes = (key_bits + digit_bits - 1u) / digit_bits;
     for (uint32_t i = threadIdx.x; i < passes * radix; i += blockDim.x) s_hist[i] = 0u;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
-        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+        for (uint32_t p = 0; p < passes; ++p) {
+            const uint32_t left = key_bits - p * digit_bits;
+            const uint32_t mask = left >= digit_bits ? radix - 1u : (1u << left) - 1u;
+            atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+        }
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < passes * radix; i += blockDim.x)
@@ -257,10 +263,10 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
                                                            const uint32_t* __restrict__ vals_in,
                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                            const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
-                                                           const uint32_t* __restrict__ hist, FrameCtl* ctl,
-                                                           uint64_t* flags, uint32_t slot) {
+                                                           uint32_t dmask, const uint32_t* __restrict__ hist,
+                                                           FrameCtl* ctl, uint64_t* flags, uint32_t slot) {
     constexpr uint32_t RADIX = 1u << BITS;
-    constexpr uint32_t MASK = RADIX - 1u;
+    const uint32_t MASK = dmask & (RADIX - 1u);  // digit mask of this pass (narrower on a last partial digit)
     constexpr uint32_t WARPS = kSortThreads / 32;
     constexpr uint32_t PER_WARP = kSortItems * 32;
     __shared__ uint32_t s_keys[kSortPartition];
@@ -441,29 +447,29 @@ void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, Fram
     k_exclusive_scan<<<parts, kScanThreads, 0, s>>>(data, n, total_dev, ctl, flags, slot);
 }
 
-void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t passes, uint32_t* hist,
+void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s) {
     uint32_t blocks = (n + 1023u) / 1024u;
     const uint32_t cap = (uint32_t)sm_count() * 4u;
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
-    k_digit_hist<<<blocks, 256, 0, s>>>(keys, n, digit_bits, passes, hist);
+    k_digit_hist<<<blocks, 256, 0, s>>>(keys, n, digit_bits, key_bits, hist);
 }
 
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
-                     const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot, int grid_cap,
-                     cudaStream_t s) {
+                     uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
+                     int grid_cap, cudaStream_t s) {
     uint32_t parts = (max_n + kSortPartition - 1u) / kSortPartition;
     const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
     if (parts > cap) parts = cap;
     if (parts == 0) parts = 1;
     if (digit_bits == 4)
-        k_onesweep<4><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, hist,
-                                                     ctl, flags, slot);
+        k_onesweep<4><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, dmask,
+                                                     hist, ctl, flags, slot);
     else
-        k_onesweep<8><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, hist,
-                                                     ctl, flags, slot);
+        k_onesweep<8><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, dmask,
+                                                     hist, ctl, flags, slot);
 }
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,

@@ -39,10 +39,10 @@ constexpr uint32_t kSortItems = 16;
 constexpr uint32_t kSortPartition = kSortThreads * kSortItems;
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
-                     const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot, int grid_cap,
-                     cudaStream_t s);
-// Digit histograms of all passes for a standalone sort.
-void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t passes, uint32_t* hist,
+                     uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
+                     int grid_cap, cudaStream_t s);
+// Digit histograms of all passes over the low key_bits bits, for a standalone sort.
+void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);
 // Standalone exclusive scan (decoupled lookback); total written to *total_dev.
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
