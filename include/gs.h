@@ -164,6 +164,19 @@ int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, 
 /* The pinned fp32 exp of the kernels, evaluated on the device (y = exp(x)). */
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
 
+/* Exclusive scan for callers that must not allocate device memory (no counterpart in the
+ * reference). Same result as gs_exclusive_scan, but it needs no context and calls no cudaMalloc,
+ * cudaFree or other allocating routine: cudaMalloc/cudaFree can synchronize the whole device, which
+ * a real-time frame loop cannot afford, and hosts that own device memory through their own arenas
+ * forbid a library from allocating behind them. d_in, d_out (n entries; may be the same buffer) and
+ * d_total (one entry, or NULL) are device buffers of the current device; work is ordered on
+ * `stream` (a cudaStream_t) and the call returns once it has finished. Scratch is a fixed device
+ * array of about 74 KB per GPU, held until the process exits; n above 2^24 (16,777,216) returns
+ * GS_ERR_INVALID. The first call on a device looks up and clears that array, so make it before any
+ * stream capture. All calls share the array: calls that overlap on the GPU (other threads, other
+ * streams) race and must be serialised by the caller. */
+int gs_exclusive_scan_static(const uint32_t* d_in, uint32_t* d_out, uint32_t n, uint32_t* d_total, void* stream);
+
 /* ---- host utilities (no GPU needed) ----------------------------------------------------------- */
 /* Camera.getUniform() (src/renderer/camera.js:87-98) with wgpu-matrix lookAt / perspective
  * (camera.js:135-142, 0..1 clip depth) restated: fills the 176-byte block for a camera at `eye`
