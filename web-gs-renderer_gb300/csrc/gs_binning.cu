@@ -303,15 +303,13 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
         for (uint32_t d = lane; d < RADIX; d += 32) s_whist[warp][d] = 0u;
         __syncwarp();
 
-        uint32_t key[kSortItems], val[kSortItems];
+        uint32_t key[kSortItems];
         uint16_t rank[kSortItems];
         const uint32_t wbase = base + warp * PER_WARP;
 #pragma unroll
         for (uint32_t k = 0; k < kSortItems; ++k) {
             const uint32_t idx = wbase + k * 32u + lane;
-            const bool ok = idx < n;
-            key[k] = ok ? keys_in[idx] : 0xFFFFFFFFu;
-            val[k] = ok ? vals_in[idx] : 0u;
+            key[k] = idx < n ? keys_in[idx] : 0xFFFFFFFFu;
         }
 #pragma unroll
         for (uint32_t k = 0; k < kSortItems; ++k) {
@@ -374,7 +372,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
         }
         __syncthreads();
 
-        // local sorted order in shared memory
+        // local sorted order in shared memory; values are read only now, straight into their slot,
+        // which keeps them out of registers during the ranking
 #pragma unroll
         for (uint32_t k = 0; k < kSortItems; ++k) {
             const uint32_t idx = wbase + k * 32u + lane;
@@ -382,7 +381,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
                 const uint32_t d = (key[k] >> shift) & MASK;
                 const uint32_t pos = s_dstart[d] + s_whist[warp][d] + rank[k];
                 s_keys[pos] = key[k];
-                s_vals[pos] = val[k];
+                s_vals[pos] = vals_in[idx];
             }
         }
         __syncthreads();

@@ -1,21 +1,78 @@
 // gs_raster.cu -- front-to-back alpha-blending tile rasterizer (src/shaders/raseter.wgsl:35-117).
 //
-// One CTA per tile, one thread per pixel (TILE x TILE threads). The tile's sorted range is walked
-// in batches of BATCH splats: the CTA votes to stop once every pixel is done (raseter.wgsl:54-68 as
-// one __syncthreads_and), stages the batch's records (position, conic, opacity, colour and the
-// alpha cut-off) in shared memory with one gather per splat, then every pixel blends the batch in
-// order. The blend follows the pinned fp32 semantics:
+// One CTA per tile, one thread per pixel; each warp owns an 8x4 block of the tile. The tile's
+// sorted range is walked in batches of BATCH splats: the CTA votes to stop once every pixel is done
+// (raseter.wgsl:54-68 as one __syncthreads_and) and stages the batch's records in shared memory
+// with one gather per splat. Every pixel then blends the batch in order with the pinned fp32
+// semantics:
 //   power = fma(-0.5, fma(a*dx, dx, (c*dy)*dy), -((b*dx)*dy)); skip if power > 0
 //   alpha = min(0.99, o * exp(power));                         skip if alpha < 1/255
 //   testT = T * (1 - alpha);                                   done if testT < 1e-4
 //   C += colour * alpha * T (one fma per channel); T = testT
-// Pixels whose power is below the splat's cut-off skip the exp: for them o*exp(power) < 1/255 is
-// certain (the cut-off is ln((1/255)/o) less 1e-3, far beyond the rounding of exp, the product
-// and logf), so the skip cannot change a result.
+//
+// Two exact shortcuts remove most of the work without changing a single output bit:
+//  * cut-off: a pixel whose power is below the splat's cut-off c_o = ln((1/255)/o) - 1e-3 skips
+//    the exp, since o*exp(power) < 1/255 is certain there (the 1e-3 margin is far beyond the
+//    rounding of exp, the product and logf);
+//  * warp cull: when staging a splat, the CTA bounds the region {power >= c_o} by the bounding box
+//    of the ellipse Q(d) <= K', Q = a dx^2 + 2b dx dy + c dy^2, K' = -2 c_o plus the worst rounding
+//    error of the pinned power formula anywhere in the tile (16 eps times the sum of the absolute
+//    terms, bounded over the tile), with det = ac - b^2 taken at its lower rounding bound. Every
+//    warp tests its 8x4 pixel block against the 32 boxes of a group in parallel (one box per lane,
+//    one ballot) and walks only the splats whose box meets its block, in range order. A skipped
+//    splat would have been rejected by every pixel of the warp at "power < c_o" (or "power > 0").
+//    Splats whose box cannot be bounded safely (non-positive-definite or non-finite values) are
+//    never culled. Contributor counts are range positions, so skipping does not change them.
 #include "gs_kernels.h"
 
 namespace gs {
 namespace {
+
+// The pinned exp restricted to the arguments the raster can reach. For an opacity o in (0, 1] the
+// cut-off is at least ln(1/255) - 1e-3 > -5.6, so every argument lies in [-5.6, 0]: no range
+// checks are needed and 2^n (n >= -9) is applied as one exact power-of-two factor, which gives the
+// same bits as pinned_expf's two-factor scaling. o = 0 (cut-off +inf) never gets here; for a NaN
+// opacity the product o * exp(.) is NaN whatever this returns, as with pinned_expf.
+__device__ __forceinline__ float raster_expf(float x) {
+    const float n = rintf(__fmul_rn(x, 0x1.715476p+0f));
+    float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
+    r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
+    float p = 0x1.a01a02p-13f;
+    p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
+    p = __fmaf_rn(p, r, 0x1.111112p-7f);
+    p = __fmaf_rn(p, r, 0x1.555556p-5f);
+    p = __fmaf_rn(p, r, 0x1.555556p-3f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
+    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
+}
+
+__device__ __forceinline__ bool finite(float v) { return fabsf(v) <= 3.0e38f; }
+
+// Conservative box (x0, x1, y0, y1) outside of which no pixel of the tile [tx0,tx1]x[ty0,ty1] can
+// reach power >= cut with the pinned arithmetic; (+inf, -inf, +inf, -inf) when no pixel can;
+// (-inf, +inf, -inf, +inf) when no safe bound exists.
+__device__ __forceinline__ float4 cull_box(float x, float y, float a, float b, float c, float cut, float tx0,
+                                           float tx1, float ty0, float ty1) {
+    const float inf = __int_as_float(0x7f800000);
+    const float4 keep_all = make_float4(-inf, inf, -inf, inf);
+    if (!(finite(x) && finite(y) && finite(a) && finite(b) && finite(c)) || cut != cut) return keep_all;
+    if (!(a > 0.0f) || !(c > 0.0f)) return keep_all;
+    const float dxm = fmaxf(fabsf(x - tx0), fabsf(x - tx1));
+    const float dym = fmaxf(fabsf(y - ty0), fabsf(y - ty1));
+    const float smax = (a * dxm * dxm + c * dym * dym + 2.0f * fabsf(b) * dxm * dym) * 1.01f;
+    if (!finite(smax)) return keep_all;
+    if (cut > 0.0f) return make_float4(inf, -inf, inf, -inf);  // power <= 0 < cut everywhere
+    const float ac = a * c, bb = b * b;
+    const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
+    if (!(det_lo > 0.0f)) return keep_all;
+    const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
+    const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
+    const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
+    if (!finite(hx) || !finite(hy)) return keep_all;
+    return make_float4(x - hx, x + hx, y - hy, y + hy);
+}
 
 template <int TILE, int BATCH>
 __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restrict__ ranges,
@@ -24,14 +81,17 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
                                                         const FrameCtl* __restrict__ ctl, uint32_t width,
                                                         uint32_t height, uint32_t tiles_x, RasterOut out) {
     constexpr int THREADS = TILE * TILE;
-    __shared__ float4 s_a[BATCH];  // (x, y, conic.x, conic.y)
-    __shared__ float4 s_b[BATCH];  // (conic.z, opacity, r, g)
-    __shared__ float2 s_c[BATCH];  // (b, cut)
+    constexpr int WX = TILE / 8;  // warps across the tile
+    __shared__ float4 s_a[BATCH];    // (x, y, conic.x, conic.y)
+    __shared__ float4 s_b[BATCH];    // (conic.z, opacity, r, g)
+    __shared__ float2 s_c[BATCH];    // (b, cut)
+    __shared__ float4 s_box[BATCH];  // cull box (x0, x1, y0, y1)
 
     const uint32_t tile = blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
-    const uint32_t lx = threadIdx.x % TILE, ly = threadIdx.x / TILE;
-    const uint32_t x = tx * TILE + lx, y = ty * TILE + ly;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 4u * (warp / WX);
+    const uint32_t x = bx0 + (lane & 7u), y = by0 + (lane >> 3);
     const bool inside = x < width && y < height;
     bool done = !inside;
     const uint2 range = reinterpret_cast<const uint2*>(ranges)[tile];
@@ -39,9 +99,12 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
     const uint32_t end = ctl ? min(range.y, ctl->sorted_count) : range.y;
     const uint32_t start = range.x;
     const float fx = (float)x, fy = (float)y;
+    const float rx0 = (float)bx0, rx1 = (float)(bx0 + 7u), ry0 = (float)by0, ry1 = (float)(by0 + 3u);
+    const float tx0 = (float)(tx * TILE), tx1 = (float)(tx * TILE + TILE - 1u);
+    const float ty0 = (float)(ty * TILE), ty1 = (float)(ty * TILE + TILE - 1u);
 
     float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;
-    uint32_t contributor = 0, last = 0;
+    uint32_t last = 0;
 
     for (uint32_t i = start; i < end; i += BATCH) {
         if (__syncthreads_and(done)) break;
@@ -55,39 +118,51 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
                     s_a[j] = r0;
                     s_b[j] = r1;
                     s_c[j] = make_float2(r2.x, r2.y);
+                    s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
                 } else {  // only after a timed-out sort: a splat that never blends
+                    const float inf = __int_as_float(0x7f800000);
                     s_a[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     s_b[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    s_c[j] = make_float2(0.0f, __int_as_float(0x7f800000));
+                    s_c[j] = make_float2(0.0f, inf);
+                    s_box[j] = make_float4(inf, -inf, inf, -inf);
                 }
             }
         }
         __syncthreads();
-        if (!done) {
-            const uint32_t cnt = min((uint32_t)BATCH, end - i);
-            for (uint32_t j = 0; j < cnt; ++j) {
-                ++contributor;
+        const uint32_t cnt = min((uint32_t)BATCH, end - i);
+        const uint32_t pos0 = i - start + 1u;  // contributor count of the batch's first splat
+        for (uint32_t g0 = 0; g0 < cnt; g0 += 32u) {
+            if (__all_sync(0xffffffffu, done)) break;
+            bool hit = false;
+            if (g0 + lane < cnt) {
+                const float4 bx = s_box[g0 + lane];
+                hit = bx.y >= rx0 && bx.x <= rx1 && bx.w >= ry0 && bx.z <= ry1;
+            }
+            uint32_t m = __ballot_sync(0xffffffffu, hit);
+            while (m) {
+                const uint32_t j = g0 + (uint32_t)(__ffs(m) - 1);
+                m &= m - 1u;
+                if (done) continue;
                 const float4 a = s_a[j];
                 const float2 c = s_c[j];
                 const float dx = a.x - fx, dy = a.y - fy;
-                const float s4 = s_b[j].x;
-                const float q = __fmaf_rn(a.z * dx, dx, (s4 * dy) * dy);
-                const float power = __fmaf_rn(-0.5f, q, -((a.w * dx) * dy));
+                const float cz = s_b[j].x;
+                const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (cz * dy) * dy), -((a.w * dx) * dy));
                 if (power > 0.0f) continue;
                 if (power < c.y) continue;
                 const float4 b = s_b[j];
-                const float alpha = fminf(kAlphaClamp, b.y * pinned_expf(power));
+                const float alpha = fminf(kAlphaClamp, b.y * raster_expf(power));
                 if (alpha < kEpsilon) continue;
                 const float testT = T * (1.0f - alpha);
                 if (testT < kBlendThreshold) {
                     done = true;
-                    break;
+                    continue;
                 }
                 cr = __fmaf_rn(b.z * alpha, T, cr);
                 cg = __fmaf_rn(b.w * alpha, T, cg);
                 cb = __fmaf_rn(c.x * alpha, T, cb);
                 T = testT;
-                last = contributor;
+                last = pos0 + j;
             }
         }
     }
@@ -113,11 +188,12 @@ void launch_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, c
                  const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
                  const RasterOut& out, cudaStream_t s) {
     const uint32_t grid = tiles_x * tiles_y;
+    constexpr int threads = TILE * TILE;
     switch (batch) {
-        case 32: k_raster<TILE, 32><<<grid, TILE * TILE, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        case 64: k_raster<TILE, 64><<<grid, TILE * TILE, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        case 128: k_raster<TILE, 128><<<grid, TILE * TILE, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        default: k_raster<TILE, 256><<<grid, TILE * TILE, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
+        case 32: k_raster<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
+        case 64: k_raster<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
+        case 128: k_raster<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
+        default: k_raster<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
     }
 }
 
