@@ -152,6 +152,14 @@ int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg);
  * 59*count floats in the packed input layout. Both in `location`. */
 int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location);
 
+/* Loss of the differentiation workload (no counterpart in the reference): L = mean|rgb - target| +
+ * lambda * (1 - mean SSIM), SSIM per channel with an 11x11 Gaussian window (sigma 1.5), zero padding,
+ * C1 = 0.01^2, C2 = 0.03^2; images H x W x 3. *loss (host, may be NULL) receives L; dl_drgb (may be
+ * NULL) receives dL/drgb. Host buffers: synchronous. Device buffers: stream-ordered unless loss is
+ * requested. */
+int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t width, uint32_t height,
+                    float lambda, double* loss, float* dl_drgb, int32_t location);
+
 /* Per-pass timings of the last profiled frame (GS_FLAG_PROFILE); *n_rows receives the count. */
 int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_rows);
 

@@ -133,3 +133,44 @@ def exclusive_scan(data: np.ndarray) -> tuple[np.ndarray, int]:
     d = np.array(data, dtype=np.uint32, copy=True)
     tot = load().oracle_exclusive_scan(d.ctypes.data, d.size)
     return d, int(tot)
+
+
+def backward_f64(view: bytes, packed: np.ndarray, count: int, dl_drgb: np.ndarray, tile: int = 16, factor: int = 64,
+                 threads: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """FP64 adjoint: (dL/d(packed attributes) as 59*count float64, the FP64 rgb image)."""
+    lib = load()
+    if not hasattr(lib, "_bwd_set"):
+        lib.oracle_backward_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_int]
+        lib.oracle_loss_l1_ssim.restype = C.c_double
+        lib.oracle_loss_l1_ssim.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p]
+        lib._bwd_set = True
+    packed = np.ascontiguousarray(packed, dtype=np.float32)
+    vb = C.create_string_buffer(view, 176)
+    w, h = (int(v) for v in np.frombuffer(view, np.float32, 2, 160))
+    dl = np.ascontiguousarray(dl_drgb, dtype=np.float64).reshape(h, w, 3)
+    grad = np.zeros(59 * count, np.float64)
+    rgb = np.zeros((h, w, 3), np.float64)
+    rc = lib.oracle_backward_f64(vb, packed.ctypes.data, count, tile, factor, dl.ctypes.data, grad.ctypes.data,
+                                 rgb.ctypes.data, _threads(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_backward_f64 failed ({rc})")
+    return grad, rgb
+
+
+def loss_l1_ssim(x: np.ndarray, y: np.ndarray, lam: float = 0.2, grad: bool = True):
+    """FP64 L1 + lam * (1 - SSIM) of H x W x 3 images, and dL/dx."""
+    lib = load()
+    backward_f64.__wrapped__ = True  # argtypes are set on first use of either function
+    if not hasattr(lib, "_bwd_set"):
+        lib.oracle_loss_l1_ssim.restype = C.c_double
+        lib.oracle_loss_l1_ssim.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p]
+        lib.oracle_backward_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_int]
+        lib._bwd_set = True
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    yy = np.ascontiguousarray(y, dtype=np.float64)
+    h, w = xx.shape[:2]
+    g = np.zeros_like(xx) if grad else None
+    val = lib.oracle_loss_l1_ssim(xx.ctypes.data, yy.ctypes.data, w, h, lam, g.ctypes.data if grad else None)
+    return float(val), g

@@ -594,3 +594,460 @@ void oracle_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_
 uint32_t oracle_exclusive_scan(uint32_t* data, uint32_t n) { return exclusive_scan(data, n); }
 
 }  // extern "C"
+
+// =====================================================================================================
+// Backward (no counterpart in the reference, which is forward-only): the FP64 adjoint of the pipeline
+// above, used to check the CUDA backward, plus the L1 + SSIM loss of the differentiation workload.
+// Conventions, stated once:
+//   * gradients flow through the fp32-before-quantization RGB; rgba8 has none;
+//   * culled Gaussians (near plane, frustum), skipped pairs (power > 0, alpha < 1/255) and splats after
+//     a pixel's termination get zero gradient; the 0.99 alpha clamp and the max(colour, 0) clamp have
+//     zero derivative where active;
+//   * the frustum-guard clamp of t.xy (preprocess.wgsl:254-255) is masked as in 3DGS: where t.x/t.z
+//     (t.y/t.z) is clamped, no gradient flows through t.x (t.y); t.z keeps its path through J;
+//   * tile rects, depth16 and sort order are piecewise constant: no gradient.
+// =====================================================================================================
+namespace {
+
+template <class T> struct Mat3T { T m[3][3]; };  // [row][col] (plain math layout, unlike Mat3)
+
+// Per-Gaussian forward quantities of preprocess.wgsl:58-144, recomputed for the backward.
+template <class T> struct GaussState {
+    bool near_ok = false;
+    T p[3], pv[4], clip[4], wden;
+    T s[3], q[4], qlen, qraw[4];  // q = normalized (x, y, z, w)
+    T R[3][3];                    // [row][col]
+    T Sigma[3][3];
+    T tx, ty, tz;
+    bool clampx, clampy;
+    T J[2][3];
+    T Wr[3][3];                   // upper-left 3x3 of the view matrix, [row][col]
+    T M[2][3];                    // J * Wr
+    T a, b, c, det;
+    T opacity;
+    T v[3], vlen, dir[3];
+    T Y[16];
+    T raw[3];                     // SH sum + 0.5 before max(., 0)
+};
+
+template <class T> T sh_basis(const T d[3], T Y[16]) {
+    const T x = d[0], y = d[1], z = d[2];
+    const T xx = x * x, yy = y * y, zz = z * z;
+    Y[0] = (T)kShC0;
+    Y[1] = -(T)kShC1 * y;
+    Y[2] = (T)kShC1 * z;
+    Y[3] = -(T)kShC1 * x;
+    Y[4] = (T)kShC2_0 * x * y;
+    Y[5] = (T)kShC2_1 * y * z;
+    Y[6] = (T)kShC2_2 * (2 * zz - xx - yy);
+    Y[7] = (T)kShC2_3 * x * z;
+    Y[8] = (T)kShC2_4 * (xx - yy);
+    Y[9] = (T)kShC3_0 * y * (3 * xx - yy);
+    Y[10] = (T)kShC3_1 * x * y * z;
+    Y[11] = (T)kShC3_2 * y * (4 * zz - xx - yy);
+    Y[12] = (T)kShC3_3 * z * (2 * zz - 3 * xx - 3 * yy);
+    Y[13] = (T)kShC3_4 * x * (4 * zz - xx - yy);
+    Y[14] = (T)kShC3_5 * z * (xx - yy);
+    Y[15] = (T)kShC3_6 * x * (xx - 3 * yy);
+    return Y[0];
+}
+
+// d(sum_k Y_k w_k)/d(x, y, z) for weights w_k.
+template <class T> void sh_basis_grad(const T d[3], const T w[16], T out[3]) {
+    const T x = d[0], y = d[1], z = d[2];
+    const T xx = x * x, yy = y * y, zz = z * z;
+    T gx = 0, gy = 0, gz = 0;
+    gy += -(T)kShC1 * w[1];
+    gz += (T)kShC1 * w[2];
+    gx += -(T)kShC1 * w[3];
+    gx += (T)kShC2_0 * y * w[4];          gy += (T)kShC2_0 * x * w[4];
+    gy += (T)kShC2_1 * z * w[5];          gz += (T)kShC2_1 * y * w[5];
+    gx += -2 * (T)kShC2_2 * x * w[6];     gy += -2 * (T)kShC2_2 * y * w[6];     gz += 4 * (T)kShC2_2 * z * w[6];
+    gx += (T)kShC2_3 * z * w[7];          gz += (T)kShC2_3 * x * w[7];
+    gx += 2 * (T)kShC2_4 * x * w[8];      gy += -2 * (T)kShC2_4 * y * w[8];
+    gx += 6 * (T)kShC3_0 * x * y * w[9];  gy += (T)kShC3_0 * (3 * xx - 3 * yy) * w[9];
+    gx += (T)kShC3_1 * y * z * w[10];     gy += (T)kShC3_1 * x * z * w[10];     gz += (T)kShC3_1 * x * y * w[10];
+    gx += -2 * (T)kShC3_2 * x * y * w[11]; gy += (T)kShC3_2 * (4 * zz - xx - 3 * yy) * w[11]; gz += 8 * (T)kShC3_2 * y * z * w[11];
+    gx += -6 * (T)kShC3_3 * x * z * w[12]; gy += -6 * (T)kShC3_3 * y * z * w[12]; gz += (T)kShC3_3 * (6 * zz - 3 * xx - 3 * yy) * w[12];
+    gx += (T)kShC3_4 * (4 * zz - 3 * xx - yy) * w[13]; gy += -2 * (T)kShC3_4 * x * y * w[13]; gz += 8 * (T)kShC3_4 * x * z * w[13];
+    gx += 2 * (T)kShC3_5 * x * z * w[14]; gy += -2 * (T)kShC3_5 * y * z * w[14]; gz += (T)kShC3_5 * (xx - yy) * w[14];
+    gx += (T)kShC3_6 * (3 * xx - 3 * yy) * w[15]; gy += -6 * (T)kShC3_6 * x * y * w[15];
+    out[0] = gx; out[1] = gy; out[2] = gz;
+}
+
+template <class T>
+GaussState<T> gauss_forward(const Uniforms& u, const float* params, uint64_t n, uint64_t g) {
+    GaussState<T> st;
+    const float* P = params;
+    for (int i = 0; i < 3; ++i) st.p[i] = P[g * 3 + i];
+    for (int i = 0; i < 4; ++i) {
+        st.pv[i] = (T)u.view[0 * 4 + i] * st.p[0] + (T)u.view[1 * 4 + i] * st.p[1] + (T)u.view[2 * 4 + i] * st.p[2] +
+                   (T)u.view[3 * 4 + i];
+        st.clip[i] = (T)u.viewProj[0 * 4 + i] * st.p[0] + (T)u.viewProj[1 * 4 + i] * st.p[1] +
+                     (T)u.viewProj[2 * 4 + i] * st.p[2] + (T)u.viewProj[3 * 4 + i];
+    }
+    st.near_ok = !(st.pv[2] >= -(T)kZNearView);
+    if (!st.near_ok) return st;
+    st.wden = st.clip[3] + (T)kSmallValue;
+    const float* sc = P + 3 * n + g * 3;
+    const float* qs = P + 6 * n + g * 4;
+    for (int i = 0; i < 3; ++i) st.s[i] = std::exp((T)sc[i]);
+    st.qraw[0] = qs[1]; st.qraw[1] = qs[2]; st.qraw[2] = qs[3]; st.qraw[3] = qs[0];
+    st.qlen = std::sqrt(st.qraw[0] * st.qraw[0] + st.qraw[1] * st.qraw[1] + st.qraw[2] * st.qraw[2] + st.qraw[3] * st.qraw[3]);
+    for (int i = 0; i < 4; ++i) st.q[i] = st.qraw[i] / st.qlen;
+    const T x = st.q[0], y = st.q[1], z = st.q[2], w = st.q[3];
+    st.R[0][0] = 1 - 2 * (y * y + z * z); st.R[0][1] = 2 * (x * y - w * z);     st.R[0][2] = 2 * (x * z + w * y);
+    st.R[1][0] = 2 * (x * y + w * z);     st.R[1][1] = 1 - 2 * (x * x + z * z); st.R[1][2] = 2 * (y * z - w * x);
+    st.R[2][0] = 2 * (x * z - w * y);     st.R[2][1] = 2 * (y * z + w * x);     st.R[2][2] = 1 - 2 * (x * x + y * y);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            T acc = 0;
+            for (int k = 0; k < 3; ++k) acc += st.R[i][k] * st.s[k] * st.s[k] * st.R[j][k];
+            st.Sigma[i][j] = acc;
+        }
+    const T limx = (T)kFrustumExtended * (T)u.tanFov[0], limy = (T)kFrustumExtended * (T)u.tanFov[1];
+    st.tz = st.pv[2];
+    const T rx = st.pv[0] / st.tz, ry = st.pv[1] / st.tz;
+    st.clampx = rx < -limx || rx > limx;
+    st.clampy = ry < -limy || ry > limy;
+    st.tx = tmin(limx, tmax(-limx, rx)) * st.tz;
+    st.ty = tmin(limy, tmax(-limy, ry)) * st.tz;
+    const T fx = (T)u.focal[0], fy = (T)u.focal[1];
+    st.J[0][0] = fx / st.tz; st.J[0][1] = 0; st.J[0][2] = -fx * st.tx / (st.tz * st.tz);
+    st.J[1][0] = 0; st.J[1][1] = fy / st.tz; st.J[1][2] = -fy * st.ty / (st.tz * st.tz);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) st.Wr[r][c] = (T)u.view[c * 4 + r];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 3; ++c) {
+            T acc = 0;
+            for (int k = 0; k < 3; ++k) acc += st.J[r][k] * st.Wr[k][c];
+            st.M[r][c] = acc;
+        }
+    T cov2[2][2];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 2; ++c) {
+            T acc = 0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) acc += st.M[r][i] * st.Sigma[i][j] * st.M[c][j];
+            cov2[r][c] = acc;
+        }
+    st.a = cov2[0][0] + (T)0.3f;
+    st.b = cov2[0][1];
+    st.c = cov2[1][1] + (T)0.3f;
+    st.det = st.a * st.c - st.b * st.b;
+    st.opacity = (T)1 / ((T)1 + std::exp(-(T)P[13 * n + g]));
+    for (int i = 0; i < 3; ++i) st.v[i] = st.p[i] - (T)u.cameraPos[i];
+    st.vlen = std::sqrt(st.v[0] * st.v[0] + st.v[1] * st.v[1] + st.v[2] * st.v[2]);
+    for (int i = 0; i < 3; ++i) st.dir[i] = st.v[i] / st.vlen;
+    sh_basis<T>(st.dir, st.Y);
+    for (int ch = 0; ch < 3; ++ch) {
+        T r = st.Y[0] * (T)P[10 * n + g * 3 + ch];
+        for (int k = 1; k < 16; ++k) r += st.Y[k] * (T)P[14 * n + g * 45 + (k - 1) + 15 * ch];
+        st.raw[ch] = r + (T)0.5f;
+    }
+    return st;
+}
+
+// dL/d(pixel.xy, conic.xyz, opacity, colour.rgb) of one Gaussian -> dL/d(packed attributes).
+template <class T>
+void gauss_backward(const Uniforms& u, const float* P, uint64_t n, uint64_t g, const T* d2, T* grad) {
+    const GaussState<T> st = gauss_forward<T>(u, P, n, g);
+    if (!st.near_ok) return;
+    T gp[3] = {0, 0, 0};
+    // colour (SH): dL/dcoef and dL/ddir
+    T gcol[3];
+    for (int ch = 0; ch < 3; ++ch) gcol[ch] = st.raw[ch] < 0 ? (T)0 : d2[6 + ch];
+    T wsh[16];
+    for (int k = 0; k < 16; ++k) {
+        T acc = 0;
+        for (int ch = 0; ch < 3; ++ch) {
+            const T coef = k == 0 ? (T)P[10 * n + g * 3 + ch] : (T)P[14 * n + g * 45 + (k - 1) + 15 * ch];
+            acc += coef * gcol[ch];
+            const T gk = st.Y[k] * gcol[ch];
+            if (k == 0) grad[10 * n + g * 3 + ch] += gk;
+            else grad[14 * n + g * 45 + (k - 1) + 15 * ch] += gk;
+        }
+        wsh[k] = acc;
+    }
+    T gdir[3];
+    sh_basis_grad<T>(st.dir, wsh, gdir);
+    const T dd = gdir[0] * st.dir[0] + gdir[1] * st.dir[1] + gdir[2] * st.dir[2];
+    for (int i = 0; i < 3; ++i) gp[i] += (gdir[i] - st.dir[i] * dd) / st.vlen;
+    // opacity
+    grad[13 * n + g] += d2[5] * st.opacity * ((T)1 - st.opacity);
+    // conic -> cov2' (a, b, c)
+    const T gA = d2[2], gB = d2[3], gC = d2[4];
+    const T det2 = st.det * st.det;
+    const T ga = gA * (-st.c * st.c / det2) + gB * (st.b * st.c / det2) + gC * (-st.b * st.b / det2);
+    const T gb = gA * (2 * st.b * st.c / det2) + gB * (-(st.a * st.c + st.b * st.b) / det2) + gC * (2 * st.a * st.b / det2);
+    const T gc = gA * (-st.b * st.b / det2) + gB * (st.b * st.a / det2) + gC * (-st.a * st.a / det2);
+    const T G2[2][2] = {{ga, gb / 2}, {gb / 2, gc}};
+    // cov2 = M Sigma M^T: dL/dSigma = M^T G2 M, dL/dM = 2 G2 M Sigma
+    T gSigma[3][3], gM[2][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            T acc = 0;
+            for (int r = 0; r < 2; ++r)
+                for (int c = 0; c < 2; ++c) acc += st.M[r][i] * G2[r][c] * st.M[c][j];
+            gSigma[i][j] = acc;
+        }
+    for (int r = 0; r < 2; ++r)
+        for (int j = 0; j < 3; ++j) {
+            T acc = 0;
+            for (int c = 0; c < 2; ++c)
+                for (int k = 0; k < 3; ++k) acc += G2[r][c] * st.M[c][k] * st.Sigma[k][j];
+            gM[r][j] = 2 * acc;
+        }
+    // M = J Wr: dL/dJ = dL/dM Wr^T
+    T gJ[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int k = 0; k < 3; ++k) {
+            T acc = 0;
+            for (int c = 0; c < 3; ++c) acc += gM[r][c] * st.Wr[k][c];
+            gJ[r][k] = acc;
+        }
+    const T fx = (T)u.focal[0], fy = (T)u.focal[1], tz = st.tz, tz2 = tz * tz, tz3 = tz2 * tz;
+    T gpv[3];
+    gpv[0] = st.clampx ? (T)0 : gJ[0][2] * (-fx / tz2);
+    gpv[1] = st.clampy ? (T)0 : gJ[1][2] * (-fy / tz2);
+    gpv[2] = gJ[0][0] * (-fx / tz2) + gJ[0][2] * (2 * fx * st.tx / tz3) + gJ[1][1] * (-fy / tz2) +
+             gJ[1][2] * (2 * fy * st.ty / tz3);
+    for (int i = 0; i < 3; ++i) gp[i] += st.Wr[0][i] * gpv[0] + st.Wr[1][i] * gpv[1] + st.Wr[2][i] * gpv[2];
+    // pixel position -> ndc -> clip -> p
+    const T gndx = d2[0] * (T)u.textureSize[0] * (T)0.5, gndy = d2[1] * (T)u.textureSize[1] * (T)0.5;
+    const T gcx = gndx / st.wden, gcy = gndy / st.wden;
+    const T gcw = -(gndx * st.clip[0] + gndy * st.clip[1]) / (st.wden * st.wden);
+    for (int i = 0; i < 3; ++i)
+        gp[i] += (T)u.viewProj[i * 4 + 0] * gcx + (T)u.viewProj[i * 4 + 1] * gcy + (T)u.viewProj[i * 4 + 3] * gcw;
+    for (int i = 0; i < 3; ++i) grad[g * 3 + i] += gp[i];
+    // Sigma = A A^T, A = R diag(s)
+    T A[3][3], gAm[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = st.R[i][j] * st.s[j];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            T acc = 0;
+            for (int k = 0; k < 3; ++k) acc += (gSigma[i][k] + gSigma[k][i]) * A[k][j];
+            gAm[i][j] = acc;
+        }
+    T gR[3][3];
+    for (int j = 0; j < 3; ++j) {
+        T gs = 0;
+        for (int i = 0; i < 3; ++i) {
+            gs += gAm[i][j] * st.R[i][j];
+            gR[i][j] = gAm[i][j] * st.s[j];
+        }
+        grad[3 * n + g * 3 + j] += gs * st.s[j];  // d s / d logscale = s
+    }
+    const T x = st.q[0], y = st.q[1], z = st.q[2], w = st.q[3];
+    T gq[4];
+    gq[0] = gR[1][0] * 2 * y + gR[2][0] * 2 * z + gR[0][1] * 2 * y + gR[1][1] * -4 * x + gR[2][1] * 2 * w +
+            gR[0][2] * 2 * z + gR[1][2] * -2 * w + gR[2][2] * -4 * x;
+    gq[1] = gR[0][0] * -4 * y + gR[1][0] * 2 * x + gR[2][0] * -2 * w + gR[0][1] * 2 * x + gR[2][1] * 2 * z +
+            gR[0][2] * 2 * w + gR[1][2] * 2 * z + gR[2][2] * -4 * y;
+    gq[2] = gR[0][0] * -4 * z + gR[1][0] * 2 * w + gR[2][0] * 2 * x + gR[0][1] * -2 * w + gR[1][1] * -4 * z +
+            gR[2][1] * 2 * y + gR[0][2] * 2 * x + gR[1][2] * 2 * y;
+    gq[3] = gR[1][0] * 2 * z + gR[2][0] * -2 * y + gR[0][1] * -2 * z + gR[2][1] * 2 * x + gR[0][2] * 2 * y +
+            gR[1][2] * -2 * x;
+    const T qd = gq[0] * st.q[0] + gq[1] * st.q[1] + gq[2] * st.q[2] + gq[3] * st.q[3];
+    T gqr[4];
+    for (int i = 0; i < 4; ++i) gqr[i] = (gq[i] - st.q[i] * qd) / st.qlen;
+    // stored (rot_0..3) = (w, x, y, z)
+    grad[6 * n + g * 4 + 0] += gqr[3];
+    grad[6 * n + g * 4 + 1] += gqr[0];
+    grad[6 * n + g * 4 + 2] += gqr[1];
+    grad[6 * n + g * 4 + 3] += gqr[2];
+}
+
+// FP64 frame with the state the adjoint needs: per-Gaussian records and the sorted binning.
+template <class T>
+void backward_frame(const Uniforms& u, const float* packed, uint32_t n, uint32_t tile, uint32_t factor,
+                    const T* dl_drgb, T* grad, T* rgb_out, int threads) {
+    Pre<T> pre;
+    preprocess<T>(u, packed, n, tile, pre, threads);
+    std::vector<uint32_t> offsets((size_t)n + 1, 0u);
+    std::copy(pre.tiles_touched.begin(), pre.tiles_touched.end(), offsets.begin());
+    const uint32_t I = exclusive_scan(offsets.data(), offsets.size());
+    const uint32_t W = (uint32_t)u.textureSize[0], H = (uint32_t)u.textureSize[1];
+    const uint32_t tpr = (W + tile - 1) / tile, tpc = (H + tile - 1) / tile;
+    const uint32_t maxI = n * factor, S = std::min(I, maxI);
+    std::vector<uint32_t> keys(S), vals(S), k2(S), v2(S);
+    emit(offsets.data(), pre.meta.data(), n, tpr, maxI, keys.data(), vals.data(), threads);
+    for (uint32_t p = 0; p < 4; ++p) {
+        radix_pass(keys.data(), vals.data(), k2.data(), v2.data(), S, 8 * p);
+        keys.swap(k2);
+        vals.swap(v2);
+    }
+    std::vector<uint32_t> ranges((size_t)tpr * tpc * 2, 0u);
+    tile_ranges(keys.data(), S, ranges.data());
+    std::vector<T> inst(9 * (size_t)S, (T)0);  // per-instance 2D gradients (each instance is in one tile)
+    const int64_t ntiles = (int64_t)tpr * tpc;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+    for (int64_t t = 0; t < ntiles; ++t) {
+        const uint32_t start = ranges[t * 2], end = ranges[t * 2 + 1];
+        const uint32_t tX = (uint32_t)(t % tpr), tY = (uint32_t)(t / tpr);
+        std::vector<uint32_t> list;
+        std::vector<T> alist, glist, tlist;
+        for (uint32_t ly = 0; ly < tile; ++ly)
+            for (uint32_t lx = 0; lx < tile; ++lx) {
+                const uint32_t x = tX * tile + lx, y = tY * tile + ly;
+                if (x >= W || y >= H) continue;
+                const T fpx = (T)(float)x, fpy = (T)(float)y;
+                list.clear(); alist.clear(); glist.clear(); tlist.clear();
+                T Tr = 1, c[3] = {0, 0, 0};
+                for (uint32_t i = start; i < end; ++i) {
+                    const uint32_t g = vals[i];
+                    const T A = pre.conic_opacity[4 * (size_t)g], B = pre.conic_opacity[4 * (size_t)g + 1],
+                            C = pre.conic_opacity[4 * (size_t)g + 2], o = pre.conic_opacity[4 * (size_t)g + 3];
+                    const T dx = pre.pixel[2 * (size_t)g] - fpx, dy = pre.pixel[2 * (size_t)g + 1] - fpy;
+                    const T power = std::fma((T)-0.5, std::fma(A * dx, dx, (C * dy) * dy), -((B * dx) * dy));
+                    if (power > 0) continue;
+                    const T G = std::exp(power);
+                    const T alpha = tmin((T)kAlphaClamp, o * G);
+                    if (alpha < (T)kEpsilon) continue;
+                    const T testT = Tr * (1 - alpha);
+                    if (testT < (T)kBlendThreshold) break;
+                    for (int k = 0; k < 3; ++k) c[k] += pre.color[4 * (size_t)g + k] * alpha * Tr;
+                    list.push_back(i); alist.push_back(alpha); glist.push_back(G); tlist.push_back(Tr);
+                    Tr = testT;
+                }
+                const size_t pidx = (size_t)y * W + x;
+                if (rgb_out)
+                    for (int k = 0; k < 3; ++k) rgb_out[3 * pidx + k] = c[k];
+                const T* dl = dl_drgb + 3 * pidx;
+                T acc[3] = {0, 0, 0}, lastA = 0, lastC[3] = {0, 0, 0};
+                for (size_t k = list.size(); k-- > 0;) {
+                    const uint32_t i = list[k];
+                    const uint32_t g = vals[i];
+                    const T alpha = alist[k], G = glist[k], Tk = tlist[k];
+                    const T* col = &pre.color[4 * (size_t)g];
+                    for (int ch = 0; ch < 3; ++ch) acc[ch] = lastA * lastC[ch] + (1 - lastA) * acc[ch];
+                    T dalpha = 0;
+                    for (int ch = 0; ch < 3; ++ch) dalpha += (col[ch] - acc[ch]) * dl[ch];
+                    dalpha *= Tk;
+                    T* ig = &inst[9 * (size_t)i];
+                    for (int ch = 0; ch < 3; ++ch) ig[6 + ch] += alpha * Tk * dl[ch];
+                    const T o = pre.conic_opacity[4 * (size_t)g + 3];
+                    if (o * G <= (T)kAlphaClamp) {  // unclamped alpha = o * G
+                        const T A = pre.conic_opacity[4 * (size_t)g], B = pre.conic_opacity[4 * (size_t)g + 1],
+                                C = pre.conic_opacity[4 * (size_t)g + 2];
+                        const T dx = pre.pixel[2 * (size_t)g] - fpx, dy = pre.pixel[2 * (size_t)g + 1] - fpy;
+                        const T gpow = dalpha * o * G;
+                        ig[0] += gpow * (-A * dx - B * dy);
+                        ig[1] += gpow * (-C * dy - B * dx);
+                        ig[2] += gpow * (T)-0.5 * dx * dx;
+                        ig[3] += gpow * -dx * dy;
+                        ig[4] += gpow * (T)-0.5 * dy * dy;
+                        ig[5] += dalpha * G;
+                    }
+                    lastA = alpha;
+                    for (int ch = 0; ch < 3; ++ch) lastC[ch] = col[ch];
+                }
+            }
+    }
+    std::vector<T> d2((size_t)n * 9, (T)0);
+    for (uint32_t i = 0; i < S; ++i)
+        for (int k = 0; k < 9; ++k) d2[9 * (size_t)vals[i] + k] += inst[9 * (size_t)i + k];
+    std::fill(grad, grad + (size_t)n * 59, (T)0);
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t gi = 0; gi < (int64_t)n; ++gi) {
+        if (pre.tiles_touched[gi] == 0) continue;
+        gauss_backward<T>(u, packed, n, (uint64_t)gi, &d2[9 * (size_t)gi], grad);
+    }
+}
+
+// L = mean|x - y| + lambda * (1 - mean SSIM), SSIM per channel with an 11x11 Gaussian window
+// (sigma 1.5, normalised), zero padding, C1 = 0.01^2, C2 = 0.03^2. Images are H x W x 3.
+struct SsimWindow {
+    double w[11];
+    SsimWindow() {
+        double s = 0;
+        for (int i = 0; i < 11; ++i) { w[i] = std::exp(-(double)((i - 5) * (i - 5)) / (2.0 * 1.5 * 1.5)); s += w[i]; }
+        for (double& v : w) v /= s;
+    }
+};
+// separable correlation with zero padding, one channel plane (H x W)
+void blur(const std::vector<double>& in, std::vector<double>& out, uint32_t W, uint32_t H, const SsimWindow& k) {
+    std::vector<double> tmp((size_t)W * H, 0.0);
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            double s = 0;
+            for (int i = -5; i <= 5; ++i) {
+                const int xx = (int)x + i;
+                if (xx >= 0 && xx < (int)W) s += k.w[i + 5] * in[(size_t)y * W + xx];
+            }
+            tmp[(size_t)y * W + x] = s;
+        }
+    out.assign((size_t)W * H, 0.0);
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            double s = 0;
+            for (int i = -5; i <= 5; ++i) {
+                const int yy = (int)y + i;
+                if (yy >= 0 && yy < (int)H) s += k.w[i + 5] * tmp[(size_t)yy * W + x];
+            }
+            out[(size_t)y * W + x] = s;
+        }
+}
+
+double loss_l1_ssim(const double* X, const double* Yi, uint32_t W, uint32_t H, double lambda, double* grad) {
+    const size_t P = (size_t)W * H;
+    const double C1 = 0.01 * 0.01, C2 = 0.03 * 0.03;
+    const SsimWindow k;
+    double l1 = 0, ssim_sum = 0;
+    for (size_t i = 0; i < 3 * P; ++i) {
+        const double d = X[i] - Yi[i];
+        l1 += std::fabs(d);
+        if (grad) grad[i] = (d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0)) / (double)(3 * P);
+    }
+    l1 /= (double)(3 * P);
+    for (int ch = 0; ch < 3; ++ch) {
+        std::vector<double> x(P), y(P), xx(P), yy(P), xy(P);
+        for (size_t i = 0; i < P; ++i) {
+            x[i] = X[3 * i + ch]; y[i] = Yi[3 * i + ch];
+            xx[i] = x[i] * x[i]; yy[i] = y[i] * y[i]; xy[i] = x[i] * y[i];
+        }
+        std::vector<double> mx, my, mxx, myy, mxy;
+        blur(x, mx, W, H, k); blur(y, my, W, H, k); blur(xx, mxx, W, H, k); blur(yy, myy, W, H, k); blur(xy, mxy, W, H, k);
+        std::vector<double> d1(P), d2(P), d3(P);  // dS/dm1, dS/dm2(=dS/dsxx), dS/dmxy(=dS/dsxy)
+        for (size_t i = 0; i < P; ++i) {
+            const double sxx = mxx[i] - mx[i] * mx[i], syy = myy[i] - my[i] * my[i], sxy = mxy[i] - mx[i] * my[i];
+            const double A1 = 2 * mx[i] * my[i] + C1, A2 = 2 * sxy + C2;
+            const double B1 = mx[i] * mx[i] + my[i] * my[i] + C1, B2 = sxx + syy + C2;
+            const double s = A1 * A2 / (B1 * B2);
+            ssim_sum += s;
+            const double ds_dmx = (2 * my[i] * A2) / (B1 * B2) - s * (2 * mx[i]) / B1;
+            const double ds_dsxx = -s / B2;
+            const double ds_dsxy = 2 * A1 / (B1 * B2);
+            d1[i] = ds_dmx + ds_dsxx * (-2 * mx[i]) + ds_dsxy * (-my[i]);
+            d2[i] = ds_dsxx;
+            d3[i] = ds_dsxy;
+        }
+        if (grad) {
+            std::vector<double> b1, b2, b3;
+            blur(d1, b1, W, H, k); blur(d2, b2, W, H, k); blur(d3, b3, W, H, k);
+            const double scale = -lambda / (double)(3 * P);
+            for (size_t i = 0; i < P; ++i) grad[3 * i + ch] += scale * (b1[i] + 2 * x[i] * b2[i] + y[i] * b3[i]);
+        }
+    }
+    return l1 + lambda * (1.0 - ssim_sum / (double)(3 * P));
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_backward_f64(const void* uniforms, const float* packed, uint32_t n, uint32_t tile, uint32_t factor,
+                        const double* dl_drgb, double* grad_packed, double* rgb_out, int threads) {
+    if (!uniforms || !dl_drgb || !grad_packed || (!packed && n) || tile == 0 || factor == 0) return 1;
+    Uniforms u;
+    std::memcpy(&u, uniforms, sizeof(u));
+    backward_frame<double>(u, packed, n, tile, factor, dl_drgb, grad_packed, rgb_out, threads <= 0 ? 1 : threads);
+    return 0;
+}
+
+double oracle_loss_l1_ssim(const double* x, const double* y, uint32_t w, uint32_t h, double lambda, double* dl_dx) {
+    return loss_l1_ssim(x, y, w, h, lambda, dl_dx);
+}
+
+}  // extern "C"

@@ -90,6 +90,9 @@ struct gs_ctx {
     DevBuf<float> rgb, final_t;
     DevBuf<uint32_t> aux_u32;
     DevBuf<float> aux_f32;
+    // backward and loss
+    DevBuf<float> grad2d, grows, dl_stage, grad_stage, loss_scratch, loss_io;
+    DevBuf<double> loss_sums;
 
     // last frame
     const gs_scene* last_scene = nullptr;
@@ -280,6 +283,8 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     for (int b = 0; b < 2; ++b) { ctx->keys[b].release(); ctx->vals[b].release(); }
     ctx->flags.release(); ctx->aux_flags.release(); ctx->ranges.release(); ctx->rgba8.release();
     ctx->n_contrib.release(); ctx->rgb.release(); ctx->final_t.release(); ctx->aux_u32.release(); ctx->aux_f32.release();
+    ctx->grad2d.release(); ctx->grows.release(); ctx->dl_stage.release(); ctx->grad_stage.release();
+    ctx->loss_scratch.release(); ctx->loss_io.release(); ctx->loss_sums.release();
     if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -396,16 +401,18 @@ int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs
     if (rc != GS_OK) return rc;
 
     const bool dev_out = out->location == GS_MEM_DEVICE;
-    // a differentiable context keeps rgb / final_t / n_contrib of the last frame for gs_backward
+    // a differentiable context keeps final_t / n_contrib of the last frame in its own buffers for
+    // gs_backward; requested device copies of them are made after the frame
     const bool keep_state = (ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE) != 0;
     RasterOut ro;
     ro.rgba8 = out->rgba8 ? (dev_out ? reinterpret_cast<uint32_t*>(out->rgba8) : ctx->rgba8.p) : nullptr;
-    ro.rgb = out->rgb ? (dev_out ? out->rgb : ctx->rgb.p) : (keep_state ? ctx->rgb.p : nullptr);
-    ro.final_t = (dev_out && out->final_t) ? out->final_t : ctx->final_t.p;
-    ro.n_contrib = (dev_out && out->n_contrib) ? out->n_contrib : ctx->n_contrib.p;
-    if (!keep_state) {
-        if (!out->final_t) ro.final_t = nullptr;
-        if (!out->n_contrib) ro.n_contrib = nullptr;
+    ro.rgb = out->rgb ? (dev_out ? out->rgb : ctx->rgb.p) : nullptr;
+    if (keep_state) {
+        ro.final_t = ctx->final_t.p;
+        ro.n_contrib = ctx->n_contrib.p;
+    } else {
+        ro.final_t = out->final_t ? (dev_out ? out->final_t : ctx->final_t.p) : nullptr;
+        ro.n_contrib = out->n_contrib ? (dev_out ? out->n_contrib : ctx->n_contrib.p) : nullptr;
     }
 
     {
@@ -451,6 +458,13 @@ int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs
     ctx->have_frame = true;
     ctx->have_timing = false;
     GS_CK(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
+    if (dev_out && keep_state) {
+        const size_t pix = (size_t)w * h;
+        if (out->final_t)
+            GS_CK(cudaMemcpyAsync(out->final_t, ctx->final_t.p, pix * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (out->n_contrib)
+            GS_CK(cudaMemcpyAsync(out->n_contrib, ctx->n_contrib.p, pix * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
 
     if (!dev_out) {
         const size_t pix = (size_t)w * h;
@@ -557,8 +571,77 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 
 int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location) {
     if (!ctx) return GS_ERR_INVALID;
-    (void)scene; (void)dl_drgb; (void)grad_packed; (void)location;
-    return fail(ctx, GS_ERR_UNSUPPORTED, "gs_backward: not built yet");
+    if (!scene || !dl_drgb || !grad_packed || (location != GS_MEM_HOST && location != GS_MEM_DEVICE))
+        return fail(ctx, GS_ERR_INVALID, "gs_backward: bad argument");
+    if (!(ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE))
+        return fail(ctx, GS_ERR_STATE, "gs_backward: context was created without GS_FLAG_DIFFERENTIABLE");
+    if (!ctx->have_frame || ctx->last_scene != scene || ctx->last_n != scene->n)
+        return fail(ctx, GS_ERR_STATE, "gs_backward: the last gs_forward on this context was not on this scene");
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    const uint32_t n = scene->n, w = ctx->width, h = ctx->height;
+    const size_t pix = (size_t)w * h;
+    GS_CK(ctx->grad2d.reserve((size_t)n * 9));
+    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
+    const float* dl = dl_drgb;
+    if (location == GS_MEM_HOST) {
+        GS_CK(ctx->dl_stage.reserve(pix * 3));
+        GS_CK(cudaMemcpyAsync(ctx->dl_stage.p, dl_drgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
+        dl = ctx->dl_stage.p;
+    }
+    if (n) GS_CK(cudaMemsetAsync(ctx->grad2d.p, 0, (size_t)n * 9 * sizeof(float), ctx->stream));
+    launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, ctx->ranges.p, ctx->vals[ctx->sorted_buf].p,
+                           ctx->rec.p, n, ctx->ctl.p, w, h, ctx->tiles_x, ctx->tiles_y, ctx->final_t.p,
+                           ctx->n_contrib.p, dl, ctx->grad2d.p, ctx->stream);
+    launch_preprocess_backward(scene->rows, scene->stride, n, ctx->view.p, ctx->counts.p, ctx->grad2d.p,
+                               ctx->grows.p, ctx->stream);
+    GS_CK(cudaGetLastError());
+    if (location == GS_MEM_DEVICE) {
+        launch_rows_to_pack(ctx->grows.p, n, scene->stride, grad_packed, ctx->stream);
+        GS_CK(cudaGetLastError());
+        return GS_OK;
+    }
+    GS_CK(ctx->grad_stage.reserve((size_t)n * kRows));
+    launch_rows_to_pack(ctx->grows.p, n, scene->stride, ctx->grad_stage.p, ctx->stream);
+    GS_CK(cudaGetLastError());
+    if (n) GS_CK(cudaMemcpyAsync(grad_packed, ctx->grad_stage.p, (size_t)n * kRows * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    return GS_OK;
+}
+
+int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t width, uint32_t height,
+                    float lambda, double* loss, float* dl_drgb, int32_t location) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!rgb || !target || width == 0 || height == 0 || height > 65535u ||
+        (location != GS_MEM_HOST && location != GS_MEM_DEVICE))
+        return fail(ctx, GS_ERR_INVALID, "gs_loss_l1_ssim: bad argument");
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    const size_t pix = (size_t)width * height;
+    GS_CK(ctx->loss_scratch.reserve(loss_scratch_floats(width, height)));
+    GS_CK(ctx->loss_sums.reserve(2));
+    const float* x = rgb;
+    const float* y = target;
+    float* dl = dl_drgb;
+    if (location == GS_MEM_HOST) {
+        GS_CK(ctx->loss_io.reserve(pix * 9));
+        float* dx = ctx->loss_io.p;
+        GS_CK(cudaMemcpyAsync(dx, rgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
+        GS_CK(cudaMemcpyAsync(dx + pix * 3, target, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
+        x = dx;
+        y = dx + pix * 3;
+        dl = dl_drgb ? dx + pix * 6 : nullptr;
+    }
+    launch_loss_l1_ssim(x, y, width, height, lambda, ctx->loss_scratch.p, ctx->loss_sums.p, dl, ctx->stream);
+    GS_CK(cudaGetLastError());
+    if (location == GS_MEM_HOST && dl_drgb)
+        GS_CK(cudaMemcpyAsync(dl_drgb, dl, pix * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    if (loss || location == GS_MEM_HOST) {
+        double sums[2] = {0.0, 0.0};
+        GS_CK(cudaMemcpyAsync(sums, ctx->loss_sums.p, sizeof(sums), cudaMemcpyDeviceToHost, ctx->stream));
+        GS_CK(cudaStreamSynchronize(ctx->stream));
+        const double count = 3.0 * (double)pix;
+        if (loss) *loss = sums[1] / count + (double)lambda * (1.0 - sums[0] / count);
+    }
+    return GS_OK;
 }
 
 // ---- building blocks -------------------------------------------------------------------------------

@@ -1,0 +1,432 @@
+// gs_backward.cu -- gradients of the splat pipeline (no counterpart in the reference, which only
+// renders). Two kernels:
+//   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
+//                         contributor, recomputing power and alpha bit for bit as the forward did
+//                         (same warp cull, same pinned arithmetic), recovering T by division, and
+//                         accumulating dL/d(pixel.xy, conic, opacity, colour) per Gaussian: the 32
+//                         lanes of a warp reduce by shuffles, one lane issues the atomics;
+//   k_preprocess_backward one thread per visible Gaussian: chain rule back through colour (SH),
+//                         sigmoid, conic inverse, 2D covariance J W Sigma W^T J^T, the rotation /
+//                         scale factorisation, and the projection, into the 59 attribute rows.
+// Conventions: gradients flow through the fp32 RGB before quantization; culled Gaussians, skipped
+// pairs and splats after a pixel's termination get none; active clamps (alpha 0.99, colour >= 0)
+// pass none; where the frustum guard clamps t.x/t.z (t.y/t.z) no gradient flows through t.x (t.y),
+// as in 3DGS.
+#include "gs_kernels.h"
+
+namespace gs {
+namespace {
+
+__device__ __forceinline__ float raster_expf_b(float x) {  // identical to the forward raster's exp
+    const float n = rintf(__fmul_rn(x, 0x1.715476p+0f));
+    float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
+    r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
+    float p = 0x1.a01a02p-13f;
+    p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
+    p = __fmaf_rn(p, r, 0x1.111112p-7f);
+    p = __fmaf_rn(p, r, 0x1.555556p-5f);
+    p = __fmaf_rn(p, r, 0x1.555556p-3f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
+    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
+}
+
+__device__ __forceinline__ bool finite_b(float v) { return fabsf(v) <= 3.0e38f; }
+
+// Same cull box as the forward raster (see gs_raster.cu for the bound).
+__device__ __forceinline__ float4 cull_box_b(float x, float y, float a, float b, float c, float cut, float tx0,
+                                             float tx1, float ty0, float ty1) {
+    const float inf = __int_as_float(0x7f800000);
+    const float4 keep_all = make_float4(-inf, inf, -inf, inf);
+    if (!(finite_b(x) && finite_b(y) && finite_b(a) && finite_b(b) && finite_b(c)) || cut != cut) return keep_all;
+    if (!(a > 0.0f) || !(c > 0.0f)) return keep_all;
+    const float dxm = fmaxf(fabsf(x - tx0), fabsf(x - tx1));
+    const float dym = fmaxf(fabsf(y - ty0), fabsf(y - ty1));
+    const float smax = (a * dxm * dxm + c * dym * dym + 2.0f * fabsf(b) * dxm * dym) * 1.01f;
+    if (!finite_b(smax)) return keep_all;
+    if (cut > 0.0f) return make_float4(inf, -inf, inf, -inf);
+    const float ac = a * c, bb = b * b;
+    const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
+    if (!(det_lo > 0.0f)) return keep_all;
+    const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
+    const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
+    const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
+    if (!finite_b(hx) || !finite_b(hy)) return keep_all;
+    return make_float4(x - hx, x + hx, y - hy, y + hy);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int TILE, int BATCH>
+__global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t* __restrict__ ranges,
+                                                                 const uint32_t* __restrict__ vals,
+                                                                 const float4* __restrict__ rec, uint32_t n,
+                                                                 const FrameCtl* __restrict__ ctl, uint32_t width,
+                                                                 uint32_t height, uint32_t tiles_x,
+                                                                 const float* __restrict__ final_t,
+                                                                 const uint32_t* __restrict__ n_contrib,
+                                                                 const float* __restrict__ dl_drgb,
+                                                                 float* __restrict__ grad2d) {
+    constexpr int WX = TILE / 8;
+    __shared__ float4 s_a[BATCH];
+    __shared__ float4 s_b[BATCH];
+    __shared__ float2 s_c[BATCH];
+    __shared__ float4 s_box[BATCH];
+    __shared__ uint32_t s_g[BATCH];
+    __shared__ uint32_t s_maxl;
+
+    const uint32_t tile = blockIdx.x;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 4u * (warp / WX);
+    const uint32_t x = bx0 + (lane & 7u), y = by0 + (lane >> 3);
+    const bool inside = x < width && y < height;
+    const uint2 range = reinterpret_cast<const uint2*>(ranges)[tile];
+    const uint32_t end = ctl ? min(range.y, ctl->sorted_count) : range.y;
+    const uint32_t start = range.x;
+    const float fx = (float)x, fy = (float)y;
+    const float rx0 = (float)bx0, rx1 = (float)(bx0 + 7u), ry0 = (float)by0, ry1 = (float)(by0 + 3u);
+    const float tx0 = (float)(tx * TILE), tx1 = (float)(tx * TILE + TILE - 1u);
+    const float ty0 = (float)(ty * TILE), ty1 = (float)(ty * TILE + TILE - 1u);
+
+    uint32_t L = 0;
+    float T = 1.0f, dr = 0.0f, dg = 0.0f, db = 0.0f;
+    if (inside) {
+        const size_t p = (size_t)y * width + x;
+        L = n_contrib[p];
+        T = final_t[p];
+        dr = dl_drgb[3 * p];
+        dg = dl_drgb[3 * p + 1];
+        db = dl_drgb[3 * p + 2];
+    }
+    if (threadIdx.x == 0) s_maxl = 0;
+    __syncthreads();
+    if (L) atomicMax(&s_maxl, L);
+    __syncthreads();
+    const uint32_t maxl = min(s_maxl, end > start ? end - start : 0u);
+    float acc_r = 0.0f, acc_g = 0.0f, acc_b = 0.0f, last_a = 0.0f, last_r = 0.0f, last_g = 0.0f, last_b = 0.0f;
+
+    // positions are 1-based within the tile range; walk batches (lo, hi] from the top down
+    for (uint32_t hi = maxl; hi > 0;) {
+        const uint32_t lo = hi > (uint32_t)BATCH ? hi - BATCH : 0u;
+        const uint32_t cnt = hi - lo;
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < cnt; j += TILE * TILE) {
+            const uint32_t g = vals[start + lo + j];
+            if (g < n) {
+                const float4 r0 = __ldg(rec + (size_t)kRecFloat4 * g);
+                const float4 r1 = __ldg(rec + (size_t)kRecFloat4 * g + 1);
+                const float4 r2 = __ldg(rec + (size_t)kRecFloat4 * g + 2);
+                s_a[j] = r0;
+                s_b[j] = r1;
+                s_c[j] = make_float2(r2.x, r2.y);
+                s_box[j] = cull_box_b(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                s_g[j] = g;
+            } else {
+                const float inf = __int_as_float(0x7f800000);
+                s_box[j] = make_float4(inf, -inf, inf, -inf);
+                s_g[j] = 0xFFFFFFFFu;
+            }
+        }
+        __syncthreads();
+        // groups of 32 from the top of the batch down, splats in a group from high to low
+        for (int gtop = (int)cnt - 1; gtop >= 0; gtop -= 32) {
+            const int gbase = gtop - 31;
+            const int jj = gbase + (int)lane;
+            bool hit = false;
+            if (jj >= 0) {
+                const float4 bx = s_box[jj];
+                hit = bx.y >= rx0 && bx.x <= rx1 && bx.w >= ry0 && bx.z <= ry1;
+            }
+            uint32_t m = __ballot_sync(0xffffffffu, hit);
+            while (m) {
+                const int bit = 31 - __clz(m);
+                m &= ~(1u << bit);
+                const int j = gbase + bit;
+                const uint32_t pos = lo + (uint32_t)j + 1u;
+                float g_px = 0.0f, g_py = 0.0f, g_a = 0.0f, g_b = 0.0f, g_c = 0.0f, g_o = 0.0f;
+                float g_r = 0.0f, g_g = 0.0f, g_bl = 0.0f;
+                bool contrib = false;
+                if (pos <= L) {
+                    const float4 a = s_a[j];
+                    const float4 b = s_b[j];
+                    const float2 c = s_c[j];
+                    const float dx = a.x - fx, dy = a.y - fy;
+                    const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
+                    if (!(power > 0.0f) && !(power < c.y)) {
+                        const float G = raster_expf_b(power);
+                        const float og = b.y * G;
+                        const float alpha = fminf(kAlphaClamp, og);
+                        if (alpha >= kEpsilon) {
+                            contrib = true;
+                            const float Tb = T / (1.0f - alpha);  // transmittance in front of this splat
+                            acc_r = last_a * last_r + (1.0f - last_a) * acc_r;
+                            acc_g = last_a * last_g + (1.0f - last_a) * acc_g;
+                            acc_b = last_a * last_b + (1.0f - last_a) * acc_b;
+                            const float w = alpha * Tb;
+                            g_r = w * dr;
+                            g_g = w * dg;
+                            g_bl = w * db;
+                            const float dalpha = Tb * ((b.z - acc_r) * dr + (b.w - acc_g) * dg + (c.x - acc_b) * db);
+                            if (og <= kAlphaClamp) {
+                                const float gp = dalpha * og;  // dL/dpower
+                                g_px = gp * (-a.z * dx - a.w * dy);
+                                g_py = gp * (-b.x * dy - a.w * dx);
+                                g_a = gp * -0.5f * dx * dx;
+                                g_b = gp * -dx * dy;
+                                g_c = gp * -0.5f * dy * dy;
+                                g_o = dalpha * G;
+                            }
+                            last_a = alpha;
+                            last_r = b.z;
+                            last_g = b.w;
+                            last_b = c.x;
+                            T = Tb;
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, contrib)) {
+                    g_px = warp_sum(g_px); g_py = warp_sum(g_py); g_a = warp_sum(g_a); g_b = warp_sum(g_b);
+                    g_c = warp_sum(g_c); g_o = warp_sum(g_o); g_r = warp_sum(g_r); g_g = warp_sum(g_g);
+                    g_bl = warp_sum(g_bl);
+                    const uint32_t gi = s_g[j];
+                    if (lane == 0 && gi < n) {
+                        float* dst = grad2d + (size_t)9 * gi;
+                        atomicAdd(dst + 0, g_px); atomicAdd(dst + 1, g_py); atomicAdd(dst + 2, g_a);
+                        atomicAdd(dst + 3, g_b); atomicAdd(dst + 4, g_c); atomicAdd(dst + 5, g_o);
+                        atomicAdd(dst + 6, g_r); atomicAdd(dst + 7, g_g); atomicAdd(dst + 8, g_bl);
+                    }
+                }
+            }
+        }
+        hi = lo;
+    }
+}
+
+// ---- preprocess backward ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
+                                                             uint32_t n, const ViewBlock* __restrict__ vb,
+                                                             const uint32_t* __restrict__ counts,
+                                                             const float* __restrict__ grad2d,
+                                                             float* __restrict__ grows) {
+    __shared__ ViewBlock sv;
+    if (threadIdx.x < 44) reinterpret_cast<uint32_t*>(&sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(vb)[threadIdx.x];
+    __syncthreads();
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    auto R_ = [&](int row) { return __ldg(rows + (size_t)row * stride + g); };
+    auto W_ = [&](int row, float v) { grows[(size_t)row * stride + g] = v; };
+    if (counts[g] == 0u) {
+        for (int r = 0; r < kRows; ++r) W_(r, 0.0f);
+        return;
+    }
+    const float* d2 = grad2d + (size_t)9 * g;
+    const float gpx = d2[0], gpy = d2[1], gA = d2[2], gB = d2[3], gC = d2[4], go = d2[5];
+    const float p[3] = {R_(0), R_(1), R_(2)};
+    float pv[4], clip[4];
+    for (int i = 0; i < 4; ++i) {
+        pv[i] = sv.view[i] * p[0] + sv.view[4 + i] * p[1] + sv.view[8 + i] * p[2] + sv.view[12 + i];
+        clip[i] = sv.viewProj[i] * p[0] + sv.viewProj[4 + i] * p[1] + sv.viewProj[8 + i] * p[2] + sv.viewProj[12 + i];
+    }
+    const float wden = clip[3] + kSmallValue;
+    // rotation and scale
+    float s[3];
+    for (int i = 0; i < 3; ++i) s[i] = pinned_expf(R_(kRowScale + i));
+    const float qr[4] = {R_(kRowQuat + 1), R_(kRowQuat + 2), R_(kRowQuat + 3), R_(kRowQuat + 0)};  // (x, y, z, w)
+    const float qlen = sqrtf(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
+    const float q[4] = {qr[0] / qlen, qr[1] / qlen, qr[2] / qlen, qr[3] / qlen};
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    float R[3][3];  // [row][col]
+    R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z);     R[0][2] = 2 * (x * z + w * y);
+    R[1][0] = 2 * (x * y + w * z);     R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
+    R[2][0] = 2 * (x * z - w * y);     R[2][1] = 2 * (y * z + w * x);     R[2][2] = 1 - 2 * (x * x + y * y);
+    float A[3][3], Sg[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = R[i][j] * s[j];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Sg[i][j] = A[i][0] * A[j][0] + A[i][1] * A[j][1] + A[i][2] * A[j][2];
+    // 2D covariance
+    const float limx = kFrustumExtended * sv.tanFov[0], limy = kFrustumExtended * sv.tanFov[1];
+    const float tz = pv[2];
+    const float rxr = pv[0] / tz, ryr = pv[1] / tz;
+    const bool clampx = rxr < -limx || rxr > limx, clampy = ryr < -limy || ryr > limy;
+    const float tx = fminf(limx, fmaxf(-limx, rxr)) * tz, ty = fminf(limy, fmaxf(-limy, ryr)) * tz;
+    const float fxl = sv.focal[0], fyl = sv.focal[1];
+    const float J[2][3] = {{fxl / tz, 0.0f, -fxl * tx / (tz * tz)}, {0.0f, fyl / tz, -fyl * ty / (tz * tz)}};
+    float Wr[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Wr[r][c] = sv.view[c * 4 + r];
+    float M[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 3; ++c) M[r][c] = J[r][0] * Wr[0][c] + J[r][1] * Wr[1][c] + J[r][2] * Wr[2][c];
+    float MS[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 3; ++c) MS[r][c] = M[r][0] * Sg[0][c] + M[r][1] * Sg[1][c] + M[r][2] * Sg[2][c];
+    const float ca = MS[0][0] * M[0][0] + MS[0][1] * M[0][1] + MS[0][2] * M[0][2] + 0.3f;
+    const float cb = MS[0][0] * M[1][0] + MS[0][1] * M[1][1] + MS[0][2] * M[1][2];
+    const float cc = MS[1][0] * M[1][0] + MS[1][1] * M[1][1] + MS[1][2] * M[1][2] + 0.3f;
+    const float det = ca * cc - cb * cb, det2 = det * det;
+    // conic -> (a, b, c)
+    const float ga = gA * (-cc * cc / det2) + gB * (cb * cc / det2) + gC * (-cb * cb / det2);
+    const float gb = gA * (2 * cb * cc / det2) + gB * (-(ca * cc + cb * cb) / det2) + gC * (2 * ca * cb / det2);
+    const float gc = gA * (-cb * cb / det2) + gB * (cb * ca / det2) + gC * (-ca * ca / det2);
+    const float G2[2][2] = {{ga, 0.5f * gb}, {0.5f * gb, gc}};
+    // dL/dSigma = M^T G2 M ; dL/dM = 2 G2 M Sigma
+    float GM[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 3; ++c) GM[r][c] = G2[r][0] * M[0][c] + G2[r][1] * M[1][c];
+    float gS[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) gS[i][j] = M[0][i] * GM[0][j] + M[1][i] * GM[1][j];
+    float gM[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 3; ++c) gM[r][c] = 2.0f * (G2[r][0] * MS[0][c] + G2[r][1] * MS[1][c]);
+    // dL/dJ = dL/dM Wr^T
+    float gJ[2][3];
+    for (int r = 0; r < 2; ++r)
+        for (int k = 0; k < 3; ++k) gJ[r][k] = gM[r][0] * Wr[k][0] + gM[r][1] * Wr[k][1] + gM[r][2] * Wr[k][2];
+    const float tz2 = tz * tz, tz3 = tz2 * tz;
+    float gpv[3];
+    gpv[0] = clampx ? 0.0f : gJ[0][2] * (-fxl / tz2);
+    gpv[1] = clampy ? 0.0f : gJ[1][2] * (-fyl / tz2);
+    gpv[2] = gJ[0][0] * (-fxl / tz2) + gJ[0][2] * (2.0f * fxl * tx / tz3) + gJ[1][1] * (-fyl / tz2) +
+             gJ[1][2] * (2.0f * fyl * ty / tz3);
+    float gp[3];
+    for (int i = 0; i < 3; ++i) gp[i] = Wr[0][i] * gpv[0] + Wr[1][i] * gpv[1] + Wr[2][i] * gpv[2];
+    // pixel position -> clip -> p
+    const float gndx = gpx * sv.textureSize[0] * 0.5f, gndy = gpy * sv.textureSize[1] * 0.5f;
+    const float gcx = gndx / wden, gcy = gndy / wden, gcw = -(gndx * clip[0] + gndy * clip[1]) / (wden * wden);
+    for (int i = 0; i < 3; ++i) gp[i] += sv.viewProj[i * 4 + 0] * gcx + sv.viewProj[i * 4 + 1] * gcy + sv.viewProj[i * 4 + 3] * gcw;
+    // colour (SH)
+    float v[3] = {p[0] - sv.cameraPos[0], p[1] - sv.cameraPos[1], p[2] - sv.cameraPos[2]};
+    const float vlen = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const float dx_ = v[0] / vlen, dy_ = v[1] / vlen, dz_ = v[2] / vlen;
+    const float xx = dx_ * dx_, yy = dy_ * dy_, zz = dz_ * dz_;
+    float Y[16];
+    Y[0] = kShC0;
+    Y[1] = -kShC1 * dy_;
+    Y[2] = kShC1 * dz_;
+    Y[3] = -kShC1 * dx_;
+    Y[4] = kShC2_0 * dx_ * dy_;
+    Y[5] = kShC2_1 * dy_ * dz_;
+    Y[6] = kShC2_2 * (2 * zz - xx - yy);
+    Y[7] = kShC2_3 * dx_ * dz_;
+    Y[8] = kShC2_4 * (xx - yy);
+    Y[9] = kShC3_0 * dy_ * (3 * xx - yy);
+    Y[10] = kShC3_1 * dx_ * dy_ * dz_;
+    Y[11] = kShC3_2 * dy_ * (4 * zz - xx - yy);
+    Y[12] = kShC3_3 * dz_ * (2 * zz - 3 * xx - 3 * yy);
+    Y[13] = kShC3_4 * dx_ * (4 * zz - xx - yy);
+    Y[14] = kShC3_5 * dz_ * (xx - yy);
+    Y[15] = kShC3_6 * dx_ * (xx - 3 * yy);
+    float gcol[3];
+    for (int ch = 0; ch < 3; ++ch) {
+        float raw = Y[0] * R_(kRowDc + ch);
+        for (int k = 1; k < 16; ++k) raw += Y[k] * R_(kRowRest + (k - 1) + 15 * ch);
+        raw += 0.5f;
+        gcol[ch] = raw < 0.0f ? 0.0f : d2[6 + ch];
+    }
+    float wsh[16];
+    for (int k = 0; k < 16; ++k) {
+        float acc = 0.0f;
+        for (int ch = 0; ch < 3; ++ch) {
+            const int row = k == 0 ? kRowDc + ch : kRowRest + (k - 1) + 15 * ch;
+            acc += R_(row) * gcol[ch];
+            W_(row, Y[k] * gcol[ch]);
+        }
+        wsh[k] = acc;
+    }
+    float gdx = 0, gdy = 0, gdz = 0;
+    gdy += -kShC1 * wsh[1];
+    gdz += kShC1 * wsh[2];
+    gdx += -kShC1 * wsh[3];
+    gdx += kShC2_0 * dy_ * wsh[4];           gdy += kShC2_0 * dx_ * wsh[4];
+    gdy += kShC2_1 * dz_ * wsh[5];           gdz += kShC2_1 * dy_ * wsh[5];
+    gdx += -2 * kShC2_2 * dx_ * wsh[6];      gdy += -2 * kShC2_2 * dy_ * wsh[6];      gdz += 4 * kShC2_2 * dz_ * wsh[6];
+    gdx += kShC2_3 * dz_ * wsh[7];           gdz += kShC2_3 * dx_ * wsh[7];
+    gdx += 2 * kShC2_4 * dx_ * wsh[8];       gdy += -2 * kShC2_4 * dy_ * wsh[8];
+    gdx += 6 * kShC3_0 * dx_ * dy_ * wsh[9]; gdy += kShC3_0 * (3 * xx - 3 * yy) * wsh[9];
+    gdx += kShC3_1 * dy_ * dz_ * wsh[10];    gdy += kShC3_1 * dx_ * dz_ * wsh[10];    gdz += kShC3_1 * dx_ * dy_ * wsh[10];
+    gdx += -2 * kShC3_2 * dx_ * dy_ * wsh[11]; gdy += kShC3_2 * (4 * zz - xx - 3 * yy) * wsh[11]; gdz += 8 * kShC3_2 * dy_ * dz_ * wsh[11];
+    gdx += -6 * kShC3_3 * dx_ * dz_ * wsh[12]; gdy += -6 * kShC3_3 * dy_ * dz_ * wsh[12]; gdz += kShC3_3 * (6 * zz - 3 * xx - 3 * yy) * wsh[12];
+    gdx += kShC3_4 * (4 * zz - 3 * xx - yy) * wsh[13]; gdy += -2 * kShC3_4 * dx_ * dy_ * wsh[13]; gdz += 8 * kShC3_4 * dx_ * dz_ * wsh[13];
+    gdx += 2 * kShC3_5 * dx_ * dz_ * wsh[14]; gdy += -2 * kShC3_5 * dy_ * dz_ * wsh[14]; gdz += kShC3_5 * (xx - yy) * wsh[14];
+    gdx += kShC3_6 * (3 * xx - 3 * yy) * wsh[15]; gdy += -6 * kShC3_6 * dx_ * dy_ * wsh[15];
+    const float ddot = gdx * dx_ + gdy * dy_ + gdz * dz_;
+    gp[0] += (gdx - dx_ * ddot) / vlen;
+    gp[1] += (gdy - dy_ * ddot) / vlen;
+    gp[2] += (gdz - dz_ * ddot) / vlen;
+    for (int i = 0; i < 3; ++i) W_(kRowPos + i, gp[i]);
+    // opacity logit
+    const float op = 1.0f / (1.0f + pinned_expf(-R_(kRowOpacity)));
+    W_(kRowOpacity, go * op * (1.0f - op));
+    // Sigma = A A^T -> A -> (R, s) -> (quaternion, log-scale)
+    float gAm[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            gAm[i][j] = (gS[i][0] + gS[0][i]) * A[0][j] + (gS[i][1] + gS[1][i]) * A[1][j] + (gS[i][2] + gS[2][i]) * A[2][j];
+    float gR[3][3];
+    for (int j = 0; j < 3; ++j) {
+        float gs = 0.0f;
+        for (int i = 0; i < 3; ++i) {
+            gs += gAm[i][j] * R[i][j];
+            gR[i][j] = gAm[i][j] * s[j];
+        }
+        W_(kRowScale + j, gs * s[j]);
+    }
+    float gq[4];
+    gq[0] = gR[1][0] * 2 * y + gR[2][0] * 2 * z + gR[0][1] * 2 * y + gR[1][1] * -4 * x + gR[2][1] * 2 * w +
+            gR[0][2] * 2 * z + gR[1][2] * -2 * w + gR[2][2] * -4 * x;
+    gq[1] = gR[0][0] * -4 * y + gR[1][0] * 2 * x + gR[2][0] * -2 * w + gR[0][1] * 2 * x + gR[2][1] * 2 * z +
+            gR[0][2] * 2 * w + gR[1][2] * 2 * z + gR[2][2] * -4 * y;
+    gq[2] = gR[0][0] * -4 * z + gR[1][0] * 2 * w + gR[2][0] * 2 * x + gR[0][1] * -2 * w + gR[1][1] * -4 * z +
+            gR[2][1] * 2 * y + gR[0][2] * 2 * x + gR[1][2] * 2 * y;
+    gq[3] = gR[1][0] * 2 * z + gR[2][0] * -2 * y + gR[0][1] * -2 * z + gR[2][1] * 2 * x + gR[0][2] * 2 * y +
+            gR[1][2] * -2 * x;
+    const float qd = gq[0] * q[0] + gq[1] * q[1] + gq[2] * q[2] + gq[3] * q[3];
+    W_(kRowQuat + 0, (gq[3] - q[3] * qd) / qlen);  // stored rot_0 = w
+    W_(kRowQuat + 1, (gq[0] - q[0] * qd) / qlen);
+    W_(kRowQuat + 2, (gq[1] - q[1] * qd) / qlen);
+    W_(kRowQuat + 3, (gq[2] - q[2] * qd) / qlen);
+}
+
+template <int TILE>
+void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
+                     const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
+                     const float* final_t, const uint32_t* n_contrib, const float* dl, float* grad2d, cudaStream_t s) {
+    const uint32_t grid = tiles_x * tiles_y;
+    constexpr int threads = TILE * TILE;
+    switch (batch) {
+        case 32: k_raster_backward<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
+        case 64: k_raster_backward<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
+        case 128: k_raster_backward<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
+        default: k_raster_backward<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
+    }
+}
+
+}  // namespace
+
+void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals,
+                            const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
+                            uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
+                            const float* dl_drgb, float* grad2d, cudaStream_t s) {
+    if (tile == 8)
+        launch_bwd_tile<8>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+    else if (tile == 32)
+        launch_bwd_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+    else
+        launch_bwd_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+}
+
+void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
+                                const uint32_t* counts, const float* grad2d, float* grows, cudaStream_t s) {
+    if (n == 0) return;
+    k_preprocess_backward<<<(n + 255u) / 256u, 256, 0, s>>>(rows, stride, n, view, counts, grad2d, grows);
+}
+
+}  // namespace gs

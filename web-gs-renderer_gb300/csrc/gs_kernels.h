@@ -64,4 +64,21 @@ void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const 
 
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
 
+// ---- backward ---------------------------------------------------------------------------------
+// grad2d: 9 floats per Gaussian, dL/d(pixel.x, pixel.y, conic.x, conic.y, conic.z, opacity, r, g, b),
+// accumulated with atomics (zero it first).
+void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals,
+                            const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
+                            uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
+                            const float* dl_drgb, float* grad2d, cudaStream_t s);
+// grad2d -> dL/d(attribute rows), one thread per Gaussian, rows laid out like the scene.
+void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
+                                const uint32_t* counts, const float* grad2d, float* grows, cudaStream_t s);
+
+// ---- L1 + SSIM loss -----------------------------------------------------------------------------
+size_t loss_scratch_floats(uint32_t width, uint32_t height);
+// sums[0] = sum of the SSIM map, sums[1] = sum |x - y| (both over W*H*3); dl may be null.
+void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_t height, float lambda,
+                         float* scratch, double* sums, float* dl, cudaStream_t s);
+
 }  // namespace gs

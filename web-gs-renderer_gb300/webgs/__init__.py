@@ -215,10 +215,23 @@ class Context:
         return {rows[i].label.decode(): {"ms": float(rows[i].ms)} for i in range(n.value)}
 
     def backward(self, scene: Scene, dl_drgb: np.ndarray) -> np.ndarray:
+        """Gradient of the last frame of `scene` (a GS_FLAG_DIFFERENTIABLE context): dL/drgb in,
+        dL/d(packed attributes) out (59*count float32)."""
         g = np.zeros(scene.count * FLOATS_PER_GAUSSIAN, np.float32)
         dl = np.ascontiguousarray(dl_drgb, dtype=np.float32)
         self._ck(library().gs_backward(self.handle, scene.handle, _ptr(dl), _ptr(g), GS_MEM_HOST))
         return g
+
+    def loss(self, rgb: np.ndarray, target: np.ndarray, lam: float = 0.2) -> tuple[float, np.ndarray]:
+        """L1 + lam * (1 - SSIM) of an H x W x 3 image against a target, and dL/drgb."""
+        x = np.ascontiguousarray(rgb, dtype=np.float32)
+        y = np.ascontiguousarray(target, dtype=np.float32)
+        h, w = x.shape[:2]
+        dl = np.empty_like(x)
+        val = C.c_double()
+        self._ck(library().gs_loss_l1_ssim(self.handle, _ptr(x), _ptr(y), w, h, lam, C.byref(val), _ptr(dl),
+                                           GS_MEM_HOST))
+        return val.value, dl
 
     def sort_pairs(self, keys: np.ndarray, vals: np.ndarray, key_bits: int = 32) -> tuple[np.ndarray, np.ndarray]:
         k = np.array(keys, dtype=np.uint32, copy=True)

@@ -94,6 +94,8 @@ SIGNATURES = [
     ("gs_get_frame_info", C.c_int, [C.c_void_p, C.POINTER(FrameInfo)]),
     ("gs_get_debug", C.c_int, [C.c_void_p, C.POINTER(Debug)]),
     ("gs_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
+    ("gs_loss_l1_ssim", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
+                                  C.POINTER(C.c_double), C.c_void_p, C.c_int32]),
     ("gs_get_timings", C.c_int, [C.c_void_p, C.POINTER(Timing), C.c_int32, C.POINTER(C.c_int32)]),
     ("gs_sort_pairs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
     ("gs_exclusive_scan", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]),
