@@ -44,6 +44,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     return ap.parse_args()
 
 
@@ -294,9 +295,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     pscene.close()
     pctx.close()
 
+    # forward + backward: frame, L1 + 0.2 (1 - SSIM) against a perturbed-scene target, gradients of
+    # all 59 attributes, everything on the device; timed like the forward
+    scene.close()
+    ctx.close()
+    fb_1080 = fwd_bwd(W.SCENE_1M, W.CAMERA_1080P, packed, args.steps, args.warmup, local_rank)
+    fb_720 = fwd_bwd(W.SCENE_500K, W.CAMERA_720P, None, args.steps, args.warmup, local_rank)
+    batched = None if args.no_batched else batched_forward(args.steps, args.warmup, local_rank)
+    batched_fb = None if args.no_batched else batched_fwd_bwd(max(3, args.steps // 5), args.warmup, local_rank)
+
     if rank != 0:
-        scene.close()
-        ctx.close()
         if dist:
             dist.destroy_process_group()
         return
@@ -335,12 +343,65 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 "h2d_bytes_per_step": 176, "d2h_bytes_per_step": pixels * 4},
         "roofline": roof, "passes": per_pass, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": launches_per_frame * args.steps,
+        "fwd_bwd": {"1M_1080p": fb_1080, "500k_720p": fb_720},
+        "batched_fwd_16_views": batched, "batched_fwd_bwd_8_views": batched_fb,
     }
     print(json.dumps(line), flush=True)
-    scene.close()
-    ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def fwd_bwd(spec, cam, packed, steps, warmup, local_rank) -> dict:
+    """ms per forward + loss + backward step on the device (CUDA events on the context stream)."""
+    import ctypes as C
+
+    import torch
+
+    import webgs
+    from webgs import _abi
+
+    lib = webgs.library()
+    if packed is None:
+        packed = spec.build()
+    view = cam.view()
+    w, h, n = cam.width, cam.height, spec.count
+    dev = f"cuda:{local_rank}"
+    ctx = webgs.Context(device=local_rank, flags=webgs.GS_FLAG_DIFFERENTIABLE)
+    target = torch.empty(h * w * 3, dtype=torch.float32, device=dev)
+    ts = ctx.upload(webgs.perturb_scene(packed, n, 99, 0.01, 0.02), n)
+    ctx.forward_device(ts, view, rgb=target.data_ptr())
+    ctx.synchronize()
+    ts.close()
+    sc = ctx.upload(packed, n)
+    rgb = torch.empty_like(target)
+    dl = torch.empty_like(target)
+    grads = torch.empty(59 * n, dtype=torch.float32, device=dev)
+    img = _abi.Image(webgs.GS_MEM_DEVICE, None, rgb.data_ptr(), None, None)
+
+    def step():
+        ctx._ck(lib.gs_forward(ctx.handle, sc.handle, C.byref(view), C.byref(img)))
+        ctx._ck(lib.gs_loss_l1_ssim(ctx.handle, rgb.data_ptr(), target.data_ptr(), w, h, 0.2, None, dl.data_ptr(),
+                                    webgs.GS_MEM_DEVICE))
+        ctx._ck(lib.gs_backward(ctx.handle, sc.handle, dl.data_ptr(), grads.data_ptr(), webgs.GS_MEM_DEVICE))
+
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    for _ in range(max(warmup, 3)):
+        step()
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    loss = C.c_double()
+    ctx._ck(lib.gs_loss_l1_ssim(ctx.handle, rgb.data_ptr(), target.data_ptr(), w, h, 0.2, C.byref(loss), None,
+                                webgs.GS_MEM_DEVICE))
+    sc.close()
+    ctx.close()
+    return {"ms_per_step": round(ms, 4), "Mpix/s": round(w * h / ms / 1e3, 2), "loss": round(loss.value, 6),
+            "workload": f"{n} Gaussians {w}x{h}, L1 + 0.2(1-SSIM) vs perturbed-scene target, grads of 59*N floats"}
 
 
 def main():
@@ -356,3 +417,137 @@ def main():
 
 if __name__ == "__main__":
     main()
+
+
+def _timed(stream, fn, steps, warmup):
+    import torch
+
+    for _ in range(max(warmup, 3)):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def batched_forward(steps, warmup, local_rank) -> dict:
+    """3 scenes (100k, 400k, 1.5M; seeds 3-5), 16 cameras on random orbits, resolutions from
+    {640x480, 1280x720, 1920x1080}: one batched launch vs 16 plain frames. The autotuner first picks
+    tile size, digit width and raster batch depth on the 400k scene with 4 of the views."""
+    import ctypes as C
+
+    import torch
+
+    import webgs
+    from webgs import _abi, workloads as W
+
+    lib = webgs.library()
+    dev = f"cuda:{local_rank}"
+    packs = [s.build() for s in W.BATCH_SCENES]
+    cams = W.orbit_cameras(16, 2024, 9.0)
+    views = [c.view() for _, c in cams]
+    t0 = time.perf_counter()
+    tuned, tuned_ms = webgs.autotune(packs[1], W.BATCH_SCENES[1].count, [views[i] for i in range(4)], iters=3,
+                                     device=local_rank)
+    tune_s = time.perf_counter() - t0
+    res = {}
+    for label, cfg in (("default", {}), ("autotuned", tuned)):
+        ctx = webgs.Context(device=local_rank, **cfg)
+        scs = [ctx.upload(p, s.count) for s, p in zip(W.BATCH_SCENES, packs)]
+        imgs = [torch.empty(c.width * c.height, dtype=torch.int32, device=dev) for _, c in cams]
+        stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+        arr = (_abi.BatchView * len(cams))()
+        for k, ((si, c), v) in enumerate(zip(cams, views)):
+            arr[k].scene = scs[si].handle
+            arr[k].view = v
+            arr[k].out = _abi.Image(webgs.GS_MEM_DEVICE, imgs[k].data_ptr(), None, None, None)
+
+        def plain():
+            for k, (si, _) in enumerate(cams):
+                ctx.forward_device(scs[si], views[k], rgba8=imgs[k].data_ptr())
+
+        def batch():
+            ctx._ck(lib.gs_forward_batch(ctx.handle, arr, len(cams)))
+
+        ms_plain = _timed(stream, plain, steps, warmup)
+        ms_batch = _timed(stream, batch, steps, warmup)
+        pix = sum(c.width * c.height for _, c in cams)
+        res[label] = {"config": cfg or {"tile_size": 16, "digit_bits": 8, "raster_batch": 256},
+                      "plain_ms_per_view": round(ms_plain / len(cams), 4),
+                      "batched_ms_per_view": round(ms_batch / len(cams), 4),
+                      "plain_Mpix_s": round(pix / ms_plain / 1e3, 1), "batched_Mpix_s": round(pix / ms_batch / 1e3, 1),
+                      "batched_over_plain": round(ms_plain / ms_batch, 3)}
+        for s in scs:
+            s.close()
+        ctx.close()
+    res["autotune"] = {"best": tuned, "best_ms_per_4_views": round(tuned_ms, 4), "sweep_s": round(tune_s, 1)}
+    return res
+
+
+def batched_fwd_bwd(steps, warmup, local_rank) -> dict:
+    """One 3M-Gaussian scene (seed 6, 128 clusters, 40^3 box), 8 cameras at 1920x1080: one batched
+    forward + 8 losses + one batched backward (gradients summed with FP32 atomics) vs 8 sequential
+    forward + loss + backward calls."""
+    import ctypes as C
+
+    import torch
+
+    import webgs
+    from webgs import _abi, workloads as W
+
+    lib = webgs.library()
+    dev = f"cuda:{local_rank}"
+    spec = W.SCENE_3M
+    packed = spec.build()
+    n = spec.count
+    cams = [c for _, c in W.orbit_cameras(8, 77, 18.0, fixed_resolution=(1920, 1080))]
+    views = [c.view() for c in cams]
+    w, h = 1920, 1080
+    ctx = webgs.Context(device=local_rank, flags=webgs.GS_FLAG_DIFFERENTIABLE)
+    ts = ctx.upload(webgs.perturb_scene(packed, n, 99, 0.01, 0.02), n)
+    targets = [torch.empty(w * h * 3, dtype=torch.float32, device=dev) for _ in views]
+    for v, t in zip(views, targets):
+        ctx.forward_device(ts, v, rgb=t.data_ptr())
+    ctx.synchronize()
+    ts.close()
+    sc = ctx.upload(packed, n)
+    rgbs = [torch.empty(w * h * 3, dtype=torch.float32, device=dev) for _ in views]
+    dls = [torch.empty_like(r) for r in rgbs]
+    grads = torch.empty(59 * n, dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    arr = (_abi.BatchView * len(views))()
+    for k, v in enumerate(views):
+        arr[k].scene = sc.handle
+        arr[k].view = v
+        arr[k].out = _abi.Image(webgs.GS_MEM_DEVICE, None, rgbs[k].data_ptr(), None, None)
+    dl_ptrs = (C.c_void_p * len(views))(*[d.data_ptr() for d in dls])
+
+    def loss(k):
+        ctx._ck(lib.gs_loss_l1_ssim(ctx.handle, rgbs[k].data_ptr(), targets[k].data_ptr(), w, h, 0.2, None,
+                                    dls[k].data_ptr(), webgs.GS_MEM_DEVICE))
+
+    def sequential():
+        for k, v in enumerate(views):
+            img = _abi.Image(webgs.GS_MEM_DEVICE, None, rgbs[k].data_ptr(), None, None)
+            ctx._ck(lib.gs_forward(ctx.handle, sc.handle, C.byref(v), C.byref(img)))
+            loss(k)
+            ctx._ck(lib.gs_backward(ctx.handle, sc.handle, dls[k].data_ptr(), grads.data_ptr(), webgs.GS_MEM_DEVICE))
+
+    def batched():
+        ctx._ck(lib.gs_forward_batch(ctx.handle, arr, len(views)))
+        for k in range(len(views)):
+            loss(k)
+        ctx._ck(lib.gs_backward_batch(ctx.handle, sc.handle, dl_ptrs, len(views), grads.data_ptr(),
+                                      webgs.GS_MEM_DEVICE))
+
+    ms_seq = _timed(stream, sequential, steps, warmup)
+    ms_bat = _timed(stream, batched, steps, warmup)
+    sc.close()
+    ctx.close()
+    return {"workload": "3M Gaussians (128 clusters, 40^3 box, seed 6), 8 x 1920x1080, L1 + 0.2(1-SSIM)",
+            "sequential_ms_per_view": round(ms_seq / len(views), 4), "batched_ms_per_view": round(ms_bat / len(views), 4),
+            "batched_over_sequential": round(ms_seq / ms_bat, 3)}

@@ -37,8 +37,8 @@ extern "C" {
 #define GS_FLAG_PROFILE 1u /* record per-pass CUDA events (the reference's GpuProfiler,
                               src/gpu/profiler.js:47-124) */
 #define GS_FLAG_NO_GRAPH 2u /* launch kernels one by one instead of replaying a CUDA graph */
-#define GS_FLAG_DIFFERENTIABLE 4u /* keep rgb, final T and last contributor of the last frame for
-                                     gs_backward (costs 20 bytes per pixel of extra writes) */
+#define GS_FLAG_DIFFERENTIABLE 4u /* keep final T and last contributor of the last frame for
+                                     gs_backward (8 bytes per pixel of extra writes) */
 
 /* GlobalUniforms (src/shaders/preprocess.wgsl:2-12), packed by renderer.js:773-797: 176 bytes,
  * f32 offsets view@0, viewProj@16, eye@32, count(u32)@35, focal@36, tanFov@38, size@40. */
@@ -142,8 +142,23 @@ uint32_t gs_scene_count(const gs_scene* scene);
  * the instance count exceeded the budget. */
 int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs_image* out);
 
+/* One view of a batch: a scene, its 176-byte view block and its outputs. */
+typedef struct gs_batch_view {
+    const gs_scene* scene;
+    gs_view view;
+    gs_image out;
+} gs_batch_view;
+
+/* Batched forward (no counterpart in the reference, which renders one view per execute()): all
+ * views, of any scenes and resolutions, are captured into one CUDA graph and forked over the
+ * context's side streams, so small views share the GPU. Every view's output must use the same
+ * location. Same results as gs_forward per view. */
+int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count);
+
 /* Counters of the last forward (synchronizes). */
 int gs_get_frame_info(gs_ctx* ctx, gs_frame_info* info);
+/* Counters of view `index` of the last gs_forward_batch (synchronizes). */
+int gs_get_batch_frame_info(gs_ctx* ctx, uint32_t index, gs_frame_info* info);
 /* Intermediates of the last forward, copied to host (synchronizes). */
 int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg);
 
@@ -151,6 +166,18 @@ int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg);
  * forward-only): dL_drgb is W*H*3 floats (gradient w.r.t. the fp32 rgb image); grad receives
  * 59*count floats in the packed input layout. Both in `location`. */
 int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location);
+
+/* Backward of views 0..count-1 of the last gs_forward_batch, all of `scene`: dl_drgb[i] is view i's
+ * dL/drgb; the gradients of all views are summed (FP32 atomics) into grad_packed. */
+int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
+                      float* grad_packed, int32_t location);
+
+/* Autotuner (no counterpart in the reference, whose constants are fixed): times gs_forward_batch of
+ * `views` over one scene for every tile size {8,16,32} x radix digit width {4,8} x raster batch
+ * depth {32,64,128,256}, `iters` frames each, and returns the fastest configuration (other fields
+ * from `base`) and its ms per batch. Creates and destroys its own contexts. */
+int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
+                uint32_t iters, gs_config* best, float* best_ms);
 
 /* Loss of the differentiation workload (no counterpart in the reference): L = mean|rgb - target| +
  * lambda * (1 - mean SSIM), SSIM per channel with an 11x11 Gaussian window (sigma 1.5), zero padding,

@@ -1,0 +1,68 @@
+"""Batched multi-view rendering (one CUDA graph over many views and scenes) and the autotuner,
+through the C ABI: every batched view equals the single-view frame bit for bit (and so the oracle),
+batched gradients equal the sum of single-view gradients."""
+import numpy as np
+import pytest
+
+import oracle
+import webgs
+from webgs import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scenes():
+    specs = [W.SceneSpec(20_000, 3, 1, 64, 20.0), W.SceneSpec(60_000, 4, 1, 64, 20.0),
+             W.SceneSpec(150_000, 5, 1, 64, 20.0)]
+    return specs, [s.build() for s in specs]
+
+
+def test_batch_equals_single_views(scenes):
+    specs, packs = scenes
+    cams = W.orbit_cameras(7, 11, 9.0, resolutions=((160, 120), (320, 180), (256, 256)))
+    with webgs.Context() as ctx:
+        sc = [ctx.upload(p, s.count) for s, p in zip(specs, packs)]
+        items = [(sc[i], cam.view()) for i, cam in cams]
+        batch = ctx.forward_batch(items, rgba8=True, rgb=True)
+        infos = [ctx.batch_frame_info(k) for k in range(len(items))]
+        again = ctx.forward_batch(items, rgba8=True, rgb=True)  # graph replay
+        for k, ((scene, view), b, b2, info) in enumerate(zip(items, batch, again, infos)):
+            single = ctx.forward(scene, view, rgba8=True, rgb=True)
+            np.testing.assert_array_equal(b["rgb"].view(np.uint32), single["rgb"].view(np.uint32))
+            np.testing.assert_array_equal(b["rgba8"], single["rgba8"])
+            np.testing.assert_array_equal(b2["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
+            assert info["instance_count"] == ctx.frame_info()["instance_count"]
+        for s in sc:
+            s.close()
+    # one batched view against the oracle directly
+    i, cam = cams[0]
+    o = oracle.forward_f32(webgs.view_bytes(cam.view()), packs[i], specs[i].count)
+    np.testing.assert_array_equal(batch[0]["rgb"].view(np.uint32), o["rgb"].view(np.uint32))
+
+
+def test_batch_backward_is_sum_of_views():
+    spec = W.SceneSpec(30_000, 6, 1, 64, 20.0)
+    packed = spec.build()
+    cams = [c for _, c in W.orbit_cameras(3, 5, 9.0, fixed_resolution=(256, 192))]
+    rng = np.random.default_rng(0)
+    dls = [rng.normal(0, 1e-3, (192, 256, 3)).astype(np.float32) for _ in cams]
+    with webgs.Context(flags=webgs.GS_FLAG_DIFFERENTIABLE) as ctx:
+        sc = ctx.upload(packed, spec.count)
+        ctx.forward_batch([(sc, c.view()) for c in cams], rgba8=False, rgb=True)
+        g_batch = ctx.backward_batch(sc, dls)
+        g_sum = np.zeros_like(g_batch, dtype=np.float64)
+        for c, dl in zip(cams, dls):
+            ctx.forward(sc, c.view(), rgba8=False)
+            g_sum += ctx.backward(sc, dl)
+        sc.close()
+    err = np.linalg.norm(g_batch - g_sum) / np.linalg.norm(g_sum)
+    assert err < 1e-5, err
+
+
+def test_autotune_picks_a_valid_configuration():
+    spec = W.SceneSpec(20_000, 7, 0)
+    views = [W.CameraSpec((0.0, 0.0, -4.0), (0, 0, 0), 60.0, 320, 240).view()]
+    cfg, ms = webgs.autotune(spec.build(), spec.count, views, iters=2)
+    assert cfg["tile_size"] in (8, 16, 32) and cfg["digit_bits"] in (4, 8)
+    assert cfg["raster_batch"] in (32, 64, 128, 256) and ms > 0

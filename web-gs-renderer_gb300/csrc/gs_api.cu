@@ -1,11 +1,12 @@
 // gs_api.cu -- the C ABI of libwebgs.so (include/gs.h).
 //
 // Replaces the reference Renderer (src/renderer/renderer.js): the context owns one CUDA stream and
-// the per-frame buffers (sized from count * MAX_INSTANCE_FACTOR like renderer.js:531-577, grown on
-// demand and kept), and gs_forward sequences the passes of renderer.js:822-932 on that stream,
-// replayed from one CUDA graph per (scene, resolution, output set). No pass reads a count back to
-// the host: the instance count travels in FrameCtl, which every later kernel reads on the device
-// (the reference's indirect dispatch, indirect_arg.wgsl).
+// per-view frame state (buffers sized from count * MAX_INSTANCE_FACTOR like renderer.js:531-577,
+// grown on demand and kept). gs_forward sequences the passes of renderer.js:822-932 on that stream,
+// replayed from one CUDA graph per (scene, resolution, output set); gs_forward_batch captures many
+// views, forked over side streams, into one graph. No pass reads a count back to the host: the
+// instance count travels in FrameCtl, which every later kernel reads on the device (the role of the
+// reference's indirect dispatch, indirect_arg.wgsl).
 #include <algorithm>
 #include <cstddef>
 #include <cstdio>
@@ -45,23 +46,63 @@ template <class T> struct DevBuf {
 
 uint32_t bitlen(uint32_t v) { return v == 0 ? 0u : 32u - (uint32_t)__builtin_clz(v); }
 
-struct GraphKey {
-    const void* scene = nullptr;
-    uint32_t n = 0, w = 0, h = 0;
-    const void* o_rgba = nullptr;
-    const void* o_rgb = nullptr;
-    const void* o_t = nullptr;
-    const void* o_c = nullptr;
-    uint64_t alloc_gen = 0;
-    bool operator==(const GraphKey& o) const {
-        return scene == o.scene && n == o.n && w == o.w && h == o.h && o_rgba == o.o_rgba && o_rgb == o.o_rgb &&
-               o_t == o.o_t && o_c == o.o_c && alloc_gen == o.alloc_gen;
+constexpr int kViewSlots = 16;
+constexpr int kSideStreams = 4;
+enum Pass { kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
+const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile ranges", "raster"};
+
+// Everything one view's frame needs on the device, and what the last frame on it was.
+struct Frame {
+    DevBuf<FrameCtl> ctl;
+    FrameCtl* h_ctl = nullptr;  // pinned readback of the counters
+    DevBuf<ViewBlock> view;
+    DevBuf<float4> rec;
+    DevBuf<uint4> meta;
+    DevBuf<uint32_t> counts, offsets;
+    DevBuf<uint32_t> keys[2], vals[2];
+    DevBuf<uint64_t> flags;
+    DevBuf<uint32_t> ranges;
+    DevBuf<uint32_t> rgba8, n_contrib;
+    DevBuf<float> rgb, final_t;
+    DevBuf<float> grad2d, dl_stage;
+    // the last frame rendered into these buffers
+    const gs_scene* scene = nullptr;
+    const ViewBlock* view_used = nullptr;  // device view block the last frame read
+    uint32_t n = 0, width = 0, height = 0, tiles_x = 0, tiles_y = 0, passes = 0, max_instance = 0;
+    int sorted_buf = 0;
+    bool valid = false;
+
+    cudaError_t init(cudaStream_t s) {
+        cudaError_t e = ctl.reserve(1);
+        if (e == cudaSuccess) e = view.reserve(1);
+        if (e == cudaSuccess) e = cudaMallocHost(&h_ctl, sizeof(FrameCtl));
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctl.p, 0, sizeof(FrameCtl), s);
+        return e;
+    }
+    void release() {
+        ctl.release(); view.release(); rec.release(); meta.release(); counts.release(); offsets.release();
+        for (int b = 0; b < 2; ++b) { keys[b].release(); vals[b].release(); }
+        flags.release(); ranges.release(); rgba8.release(); n_contrib.release(); rgb.release(); final_t.release();
+        grad2d.release(); dl_stage.release();
+        if (h_ctl) cudaFreeHost(h_ctl);
+        h_ctl = nullptr;
     }
 };
 
-constexpr int kViewSlots = 16;
-enum Pass { kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
-const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile ranges", "raster"};
+// Launch description of one frame.
+struct FrameArgs {
+    const gs_scene* scene;
+    const ViewBlock* view;  // device copy of the view block
+    uint32_t n, w, h, tiles_x, tiles_y, passes, max_instance;
+    RasterOut out;
+};
+
+struct GraphKey {
+    std::vector<const void*> ptrs;
+    std::vector<uint32_t> dims;
+    uint64_t alloc_gen = 0;
+    bool operator==(const GraphKey& o) const { return ptrs == o.ptrs && dims == o.dims && alloc_gen == o.alloc_gen; }
+};
 
 }  // namespace
 
@@ -75,41 +116,36 @@ struct gs_scene {
 struct gs_ctx {
     gs_config cfg{};
     cudaStream_t stream = nullptr;
+    cudaStream_t side[kSideStreams] = {};
+    cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     std::string err;
 
-    DevBuf<FrameCtl> ctl, aux_ctl;
-    FrameCtl* h_ctl = nullptr;  // pinned readback of the counters
-    DevBuf<ViewBlock> view;
-    DevBuf<float4> rec;
-    DevBuf<uint4> meta;
-    DevBuf<uint32_t> counts, offsets;
-    DevBuf<uint32_t> keys[2], vals[2];
-    DevBuf<uint64_t> flags, aux_flags;
-    DevBuf<uint32_t> ranges;
-    DevBuf<uint32_t> rgba8, n_contrib;
-    DevBuf<float> rgb, final_t;
+    Frame main;                  // gs_forward / gs_backward
+    std::vector<Frame*> batch;   // gs_forward_batch / gs_backward_batch, one per view
+    uint32_t batch_count = 0;    // views of the last batch
+    uint64_t alloc_gen = 0;      // changes whenever a frame buffer is reallocated
+
+    DevBuf<FrameCtl> aux_ctl;
+    DevBuf<uint64_t> aux_flags;
     DevBuf<uint32_t> aux_u32;
     DevBuf<float> aux_f32;
-    // backward and loss
-    DevBuf<float> grad2d, grows, dl_stage, grad_stage, loss_scratch, loss_io;
+    DevBuf<float> grows, grad_stage, loss_scratch, loss_io;
     DevBuf<double> loss_sums;
+    FrameCtl* h_aux = nullptr;
 
-    // last frame
-    const gs_scene* last_scene = nullptr;
-    uint32_t last_n = 0, width = 0, height = 0, tiles_x = 0, tiles_y = 0, passes = 0, max_instance = 0;
-    int sorted_buf = 0;
-    bool have_frame = false;
+    // graph caches
+    cudaGraphExec_t exec = nullptr, exec_batch = nullptr;
+    GraphKey key, key_batch;
 
-    // graph cache (alloc_gen changes whenever a frame buffer is reallocated)
-    uint64_t alloc_gen = 0;
-    cudaGraphExec_t exec = nullptr;
-    GraphKey key{};
-
-    // pinned ring of view blocks: the H2D copy of a frame's 176-byte view reads from a slot that is
-    // not rewritten until that copy has completed (slot_done), so frames never block the host
+    // pinned view blocks: a frame's H2D copy reads a slot that is not rewritten before the copy has
+    // completed (slot_done), so frames never block the host
     ViewBlock* h_views = nullptr;
     cudaEvent_t slot_done[kViewSlots] = {};
     uint32_t next_slot = 0;
+    ViewBlock* h_bviews = nullptr;  // batch view blocks (pinned), capacity bviews_cap
+    uint32_t bviews_cap = 0;
+    cudaEvent_t bviews_done = nullptr;
+    DevBuf<ViewBlock> d_bviews;
 
     // profiling
     cudaEvent_t ev[kPassCount + 1] = {};
@@ -146,74 +182,186 @@ bool valid_config(const gs_config& c) {
     return tile_ok && digit_ok && batch_ok && c.max_instance_factor >= 1;
 }
 
-// Grows the per-frame buffers for a frame of n Gaussians and `tiles` tiles of w x h pixels.
-int ensure_frame_buffers(gs_ctx* ctx, uint32_t n, uint64_t max_instance, uint32_t tiles, uint32_t w, uint32_t h) {
+// Checks a view block and derives the frame's sizes.
+int frame_args(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, FrameArgs* a) {
+    if (!scene || scene->ctx != ctx || !view) return fail(ctx, GS_ERR_INVALID, "null scene or view");
+    const float fw = view->texture_size[0], fh = view->texture_size[1];
+    if (!(fw >= 1.0f) || !(fh >= 1.0f) || !(fw <= 65536.0f) || !(fh <= 65536.0f))
+        return fail(ctx, GS_ERR_INVALID, "texture size out of range");
+    const uint32_t w = (uint32_t)fw, h = (uint32_t)fh, tile = ctx->cfg.tile_size;
+    const uint32_t tiles_x = (w + tile - 1) / tile, tiles_y = (h + tile - 1) / tile;
+    const uint64_t tiles = (uint64_t)tiles_x * tiles_y;
+    if (tiles > 65536u) return fail(ctx, GS_ERR_INVALID, "more than 65536 tiles do not fit the key's 16-bit tile field");
+    a->scene = scene;
+    a->view = nullptr;
+    a->n = scene->n;
+    a->w = w;
+    a->h = h;
+    a->tiles_x = tiles_x;
+    a->tiles_y = tiles_y;
+    a->max_instance = scene->n * ctx->cfg.max_instance_factor;
+    const uint32_t key_bits = 16u + bitlen((uint32_t)tiles - 1u);
+    a->passes = (key_bits + ctx->cfg.digit_bits - 1) / ctx->cfg.digit_bits;
+    return GS_OK;
+}
+
+// Grows a frame's buffers for the frame described by a.
+int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     const uint32_t radix = 1u << ctx->cfg.digit_bits;
-    const void* before[] = {ctx->rec.p, ctx->meta.p, ctx->counts.p, ctx->offsets.p, ctx->keys[0].p, ctx->keys[1].p,
-                            ctx->vals[0].p, ctx->vals[1].p, ctx->flags.p, ctx->ranges.p, ctx->rgba8.p, ctx->rgb.p,
-                            ctx->final_t.p, ctx->n_contrib.p};
-    GS_CK(ctx->rec.reserve((size_t)n * kRecFloat4));
-    GS_CK(ctx->meta.reserve(n));
-    GS_CK(ctx->counts.reserve(((size_t)n + 1 + 7) / 8 * 8));
-    GS_CK(ctx->offsets.reserve((size_t)n + 1));
+    const void* before[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
+                            f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p};
+    GS_CK(f.rec.reserve((size_t)a.n * kRecFloat4));
+    GS_CK(f.meta.reserve(a.n));
+    GS_CK(f.counts.reserve(((size_t)a.n + 1 + 7) / 8 * 8));
+    GS_CK(f.offsets.reserve((size_t)a.n + 1));
     for (int b = 0; b < 2; ++b) {
-        GS_CK(ctx->keys[b].reserve(max_instance));
-        GS_CK(ctx->vals[b].reserve(max_instance));
+        GS_CK(f.keys[b].reserve(a.max_instance));
+        GS_CK(f.vals[b].reserve(a.max_instance));
     }
-    const size_t sort_parts = (max_instance + kSortPartition - 1) / kSortPartition;
-    const size_t scan_parts = ((size_t)n + 1 + kScanPartition - 1) / kScanPartition;
+    const size_t sort_parts = ((size_t)a.max_instance + kSortPartition - 1) / kSortPartition;
+    const size_t scan_parts = ((size_t)a.n + 1 + kScanPartition - 1) / kScanPartition;
     const size_t words = std::max(sort_parts * radix, scan_parts);
-    if (words > ctx->flags.cap || !ctx->flags.p) {
-        GS_CK(ctx->flags.reserve(words));
-        GS_CK(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.cap * sizeof(uint64_t), ctx->stream));
+    if (words > f.flags.cap || !f.flags.p) {
+        GS_CK(f.flags.reserve(words));
+        GS_CK(cudaMemsetAsync(f.flags.p, 0, f.flags.cap * sizeof(uint64_t), ctx->stream));
     }
-    GS_CK(ctx->ranges.reserve((size_t)tiles * 2));
-    const size_t pix = (size_t)w * h;
-    GS_CK(ctx->rgba8.reserve(pix));
-    GS_CK(ctx->rgb.reserve(pix * 3));
-    GS_CK(ctx->final_t.reserve(pix));
-    GS_CK(ctx->n_contrib.reserve(pix));
-    const void* after[] = {ctx->rec.p, ctx->meta.p, ctx->counts.p, ctx->offsets.p, ctx->keys[0].p, ctx->keys[1].p,
-                           ctx->vals[0].p, ctx->vals[1].p, ctx->flags.p, ctx->ranges.p, ctx->rgba8.p, ctx->rgb.p,
-                           ctx->final_t.p, ctx->n_contrib.p};
+    GS_CK(f.ranges.reserve((size_t)a.tiles_x * a.tiles_y * 2));
+    const size_t pix = (size_t)a.w * a.h;
+    GS_CK(f.rgba8.reserve(pix));
+    GS_CK(f.rgb.reserve(pix * 3));
+    GS_CK(f.final_t.reserve(pix));
+    GS_CK(f.n_contrib.reserve(pix));
+    const void* after[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
+                           f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) ++ctx->alloc_gen;
     return GS_OK;
 }
 
-struct FrameArgs {
-    const gs_scene* scene;
-    uint32_t n, w, h, tiles_x, tiles_y, passes, max_instance;
-    RasterOut out;
-};
+// Raster outputs of a frame: caller device buffers, or the frame's own buffers for host outputs and
+// for the state a differentiable context keeps (final T and last contributor).
+RasterOut raster_out(const gs_ctx* ctx, Frame& f, const gs_image* out) {
+    const bool dev = out && out->location == GS_MEM_DEVICE;
+    const bool keep = (ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE) != 0;
+    RasterOut ro{};
+    if (out) {
+        ro.rgba8 = out->rgba8 ? (dev ? reinterpret_cast<uint32_t*>(out->rgba8) : f.rgba8.p) : nullptr;
+        ro.rgb = out->rgb ? (dev ? out->rgb : f.rgb.p) : nullptr;
+    }
+    if (keep) {
+        ro.final_t = f.final_t.p;
+        ro.n_contrib = f.n_contrib.p;
+    } else if (out) {
+        ro.final_t = out->final_t ? (dev ? out->final_t : f.final_t.p) : nullptr;
+        ro.n_contrib = out->n_contrib ? (dev ? out->n_contrib : f.n_contrib.p) : nullptr;
+    }
+    return ro;
+}
 
-// Enqueues one frame (renderer.js:822-932) on the context stream.
-void enqueue_frame(gs_ctx* ctx, const FrameArgs& a, bool profile) {
-    cudaStream_t s = ctx->stream;
+// Enqueues one frame (renderer.js:822-932) on stream s.
+void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bool profile) {
     const uint32_t bits = ctx->cfg.digit_bits, radix = 1u << bits;
-    FrameCtl* ctl = ctx->ctl.p;
+    FrameCtl* ctl = f.ctl.p;
     if (profile) cudaEventRecord(ctx->ev[0], s);
     launch_frame_begin(ctl, s);
-    launch_preprocess(a.scene->rows, a.scene->stride, a.n, ctx->view.p, ctx->cfg.tile_size, ctx->rec.p, ctx->meta.p,
-                      ctx->counts.p, ctl, s);
+    launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p, f.counts.p,
+                      ctl, s);
     if (profile) cudaEventRecord(ctx->ev[1], s);
-    launch_scan_emit(ctx->counts.p, ctx->meta.p, a.n, a.tiles_x, a.max_instance, bits, a.passes, ctx->offsets.p,
-                     ctx->keys[0].p, ctx->vals[0].p, ctl, ctx->flags.p, 0, s);
+    launch_scan_emit(f.counts.p, f.meta.p, a.n, a.tiles_x, a.max_instance, bits, a.passes, f.offsets.p, f.keys[0].p,
+                     f.vals[0].p, ctl, f.flags.p, 0, s);
     if (profile) cudaEventRecord(ctx->ev[2], s);
     int cur = 0;
     for (uint32_t p = 0; p < a.passes; ++p) {
-        launch_onesweep(bits, ctx->keys[cur].p, ctx->vals[cur].p, ctx->keys[cur ^ 1].p, ctx->vals[cur ^ 1].p,
-                        &ctl->sorted_count, 0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl,
-                        ctx->flags.p, 1 + p, 0, s);
+        launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
+                        0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s);
         cur ^= 1;
     }
-    ctx->sorted_buf = cur;
     if (profile) cudaEventRecord(ctx->ev[3], s);
-    cudaMemsetAsync(ctx->ranges.p, 0, (size_t)a.tiles_x * a.tiles_y * 2 * sizeof(uint32_t), s);
-    launch_tile_ranges(ctx->keys[cur].p, ctl, a.tiles_x * a.tiles_y, ctx->ranges.p, 0, s);
+    cudaMemsetAsync(f.ranges.p, 0, (size_t)a.tiles_x * a.tiles_y * 2 * sizeof(uint32_t), s);
+    launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, 0, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
-    launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, ctx->ranges.p, ctx->vals[cur].p, ctx->rec.p, a.n, ctl,
-                  a.w, a.h, a.tiles_x, a.tiles_y, a.out, s);
+    launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,
+                  a.tiles_x, a.tiles_y, a.out, s);
     if (profile) cudaEventRecord(ctx->ev[5], s);
+}
+
+void remember(Frame& f, const FrameArgs& a) {
+    f.scene = a.scene;
+    f.view_used = a.view;
+    f.n = a.n;
+    f.width = a.w;
+    f.height = a.h;
+    f.tiles_x = a.tiles_x;
+    f.tiles_y = a.tiles_y;
+    f.passes = a.passes;
+    f.max_instance = a.max_instance;
+    f.sorted_buf = (int)(a.passes & 1u);
+    f.valid = true;
+}
+
+// Copies a frame's requested outputs out of its own buffers after the frame (stream-ordered).
+int copy_outputs(gs_ctx* ctx, Frame& f, const gs_image* out, cudaStream_t s) {
+    const size_t pix = (size_t)f.width * f.height;
+    if (out->location == GS_MEM_DEVICE) {
+        if (ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE) {
+            if (out->final_t) GS_CK(cudaMemcpyAsync(out->final_t, f.final_t.p, pix * 4, cudaMemcpyDeviceToDevice, s));
+            if (out->n_contrib)
+                GS_CK(cudaMemcpyAsync(out->n_contrib, f.n_contrib.p, pix * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        return GS_OK;
+    }
+    if (out->rgba8) GS_CK(cudaMemcpyAsync(out->rgba8, f.rgba8.p, pix * 4, cudaMemcpyDeviceToHost, s));
+    if (out->rgb) GS_CK(cudaMemcpyAsync(out->rgb, f.rgb.p, pix * 12, cudaMemcpyDeviceToHost, s));
+    if (out->final_t) GS_CK(cudaMemcpyAsync(out->final_t, f.final_t.p, pix * 4, cudaMemcpyDeviceToHost, s));
+    if (out->n_contrib) GS_CK(cudaMemcpyAsync(out->n_contrib, f.n_contrib.p, pix * 4, cudaMemcpyDeviceToHost, s));
+    return GS_OK;
+}
+
+int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, const GraphKey& key,
+                       const std::vector<Frame*>& frames, const std::vector<FrameArgs>& args) {
+    if (!*exec || !(key == *cached)) {
+        if (*exec) cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+        cudaGraph_t g = nullptr;
+        GS_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        if (frames.size() == 1) {
+            enqueue_frame(ctx, *frames[0], args[0], ctx->stream, false);
+        } else {
+            // views are independent: fork them over the side streams so small views fill the GPU together
+            cudaEventRecord(ctx->fork, ctx->stream);
+            const int used = (int)std::min<size_t>(frames.size(), kSideStreams);
+            for (int s = 0; s < used; ++s) cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0);
+            for (size_t i = 0; i < frames.size(); ++i) enqueue_frame(ctx, *frames[i], args[i], ctx->side[i % used], false);
+            for (int s = 0; s < used; ++s) {
+                cudaEventRecord(ctx->join[s], ctx->side[s]);
+                cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0);
+            }
+        }
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+        e = cudaGraphInstantiate(exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            *exec = nullptr;
+            return cuda_fail(ctx, e, "graph instantiate");
+        }
+        *cached = key;
+    }
+    GS_CK(cudaGraphLaunch(*exec, ctx->stream));
+    return GS_OK;
+}
+
+void drop_graphs_of_scene(gs_ctx* ctx, const gs_scene* scene) {
+    auto uses = [&](const GraphKey& k) { return std::find(k.ptrs.begin(), k.ptrs.end(), scene) != k.ptrs.end(); };
+    if (ctx->exec && uses(ctx->key)) {
+        cudaGraphExecDestroy(ctx->exec);
+        ctx->exec = nullptr;
+        ctx->key = GraphKey{};
+    }
+    if (ctx->exec_batch && uses(ctx->key_batch)) {
+        cudaGraphExecDestroy(ctx->exec_batch);
+        ctx->exec_batch = nullptr;
+        ctx->key_batch = GraphKey{};
+    }
 }
 
 }  // namespace
@@ -221,7 +369,7 @@ void enqueue_frame(gs_ctx* ctx, const FrameArgs& a, bool profile) {
 // =====================================================================================================
 extern "C" {
 
-const char* gs_version(void) { return "webgs-gb300 0.1 (sm_103a)"; }
+const char* gs_version(void) { return "webgs-gb300 0.2 (sm_103a)"; }
 
 void gs_config_default(gs_config* cfg) {
     if (!cfg) return;
@@ -248,15 +396,19 @@ int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
     if (cudaSetDevice(c.device) != cudaSuccess) return GS_ERR_CUDA;
     gs_ctx* ctx = new gs_ctx();
     ctx->cfg = c;
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        ctx->ctl.reserve(1) != cudaSuccess || ctx->aux_ctl.reserve(1) != cudaSuccess ||
-        ctx->view.reserve(1) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_ctl, sizeof(FrameCtl)) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_views, sizeof(ViewBlock) * kViewSlots) != cudaSuccess) {
+    bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (int s = 0; ok && s < kSideStreams; ++s)
+        ok = cudaStreamCreateWithFlags(&ctx->side[s], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->join[s], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ctx->bviews_done, cudaEventDisableTiming) == cudaSuccess &&
+         ctx->main.init(ctx->stream) == cudaSuccess && ctx->aux_ctl.reserve(1) == cudaSuccess &&
+         cudaMallocHost(&ctx->h_aux, sizeof(FrameCtl)) == cudaSuccess &&
+         cudaMallocHost(&ctx->h_views, sizeof(ViewBlock) * kViewSlots) == cudaSuccess;
+    if (!ok) {
         gs_ctx_destroy(ctx);
         return GS_ERR_OOM;
     }
-    cudaMemsetAsync(ctx->ctl.p, 0, sizeof(FrameCtl), ctx->stream);
     cudaMemsetAsync(ctx->aux_ctl.p, 0, sizeof(FrameCtl), ctx->stream);
     for (auto& e : ctx->ev) cudaEventCreate(&e);
     for (auto& e : ctx->slot_done) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -273,19 +425,28 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     cudaSetDevice(ctx->cfg.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
+    if (ctx->exec_batch) cudaGraphExecDestroy(ctx->exec_batch);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->slot_done)
         if (e) cudaEventDestroy(e);
+    for (int s = 0; s < kSideStreams; ++s) {
+        if (ctx->side[s]) cudaStreamDestroy(ctx->side[s]);
+        if (ctx->join[s]) cudaEventDestroy(ctx->join[s]);
+    }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->bviews_done) cudaEventDestroy(ctx->bviews_done);
     if (ctx->h_views) cudaFreeHost(ctx->h_views);
-    ctx->ctl.release(); ctx->aux_ctl.release(); ctx->view.release(); ctx->rec.release(); ctx->meta.release();
-    ctx->counts.release(); ctx->offsets.release();
-    for (int b = 0; b < 2; ++b) { ctx->keys[b].release(); ctx->vals[b].release(); }
-    ctx->flags.release(); ctx->aux_flags.release(); ctx->ranges.release(); ctx->rgba8.release();
-    ctx->n_contrib.release(); ctx->rgb.release(); ctx->final_t.release(); ctx->aux_u32.release(); ctx->aux_f32.release();
-    ctx->grad2d.release(); ctx->grows.release(); ctx->dl_stage.release(); ctx->grad_stage.release();
-    ctx->loss_scratch.release(); ctx->loss_io.release(); ctx->loss_sums.release();
-    if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+    if (ctx->h_bviews) cudaFreeHost(ctx->h_bviews);
+    if (ctx->h_aux) cudaFreeHost(ctx->h_aux);
+    ctx->main.release();
+    for (Frame* f : ctx->batch) {
+        f->release();
+        delete f;
+    }
+    ctx->aux_ctl.release(); ctx->aux_flags.release(); ctx->aux_u32.release(); ctx->aux_f32.release();
+    ctx->grows.release(); ctx->grad_stage.release(); ctx->loss_scratch.release(); ctx->loss_io.release();
+    ctx->loss_sums.release(); ctx->d_bviews.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GS_OK;
@@ -361,15 +522,10 @@ int gs_scene_destroy(gs_scene* scene) {
     if (ctx) {
         cudaSetDevice(ctx->cfg.device);
         cudaStreamSynchronize(ctx->stream);
-        if (ctx->key.scene == scene) {
-            if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
-            ctx->exec = nullptr;
-            ctx->key = GraphKey{};
-        }
-        if (ctx->last_scene == scene) {
-            ctx->last_scene = nullptr;
-            ctx->have_frame = false;
-        }
+        drop_graphs_of_scene(ctx, scene);
+        if (ctx->main.scene == scene) ctx->main.valid = false;
+        for (Frame* f : ctx->batch)
+            if (f->scene == scene) f->valid = false;
     }
     if (scene->rows) cudaFree(scene->rows);
     delete scene;
@@ -381,141 +537,173 @@ uint32_t gs_scene_count(const gs_scene* scene) { return scene ? scene->n : 0u; }
 // ---- forward ---------------------------------------------------------------------------------------
 int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs_image* out) {
     if (!ctx) return GS_ERR_INVALID;
-    if (!scene || scene->ctx != ctx || !view || !out) return fail(ctx, GS_ERR_INVALID, "gs_forward: null argument");
+    if (!out) return fail(ctx, GS_ERR_INVALID, "gs_forward: null output");
     if (out->location != GS_MEM_HOST && out->location != GS_MEM_DEVICE)
         return fail(ctx, GS_ERR_INVALID, "gs_forward: bad output location");
-    const float fw = view->texture_size[0], fh = view->texture_size[1];
-    if (!(fw >= 1.0f) || !(fh >= 1.0f) || !(fw <= 65536.0f) || !(fh <= 65536.0f))
-        return fail(ctx, GS_ERR_INVALID, "gs_forward: texture size out of range");
-    const uint32_t w = (uint32_t)fw, h = (uint32_t)fh, tile = ctx->cfg.tile_size;
-    const uint32_t tiles_x = (w + tile - 1) / tile, tiles_y = (h + tile - 1) / tile;
-    const uint64_t tiles = (uint64_t)tiles_x * tiles_y;
-    if (tiles > 65536u)
-        return fail(ctx, GS_ERR_INVALID, "gs_forward: more than 65536 tiles do not fit the key's 16-bit tile field");
-    const uint32_t n = scene->n;
-    const uint32_t max_instance = n * ctx->cfg.max_instance_factor;
-    const uint32_t key_bits = 16u + bitlen((uint32_t)tiles - 1u);
-    const uint32_t passes = (key_bits + ctx->cfg.digit_bits - 1) / ctx->cfg.digit_bits;
-    GS_CK(cudaSetDevice(ctx->cfg.device));
-    int rc = ensure_frame_buffers(ctx, n, max_instance, (uint32_t)tiles, w, h);
+    FrameArgs a;
+    int rc = frame_args(ctx, scene, view, &a);
     if (rc != GS_OK) return rc;
-
-    const bool dev_out = out->location == GS_MEM_DEVICE;
-    // a differentiable context keeps final_t / n_contrib of the last frame in its own buffers for
-    // gs_backward; requested device copies of them are made after the frame
-    const bool keep_state = (ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE) != 0;
-    RasterOut ro;
-    ro.rgba8 = out->rgba8 ? (dev_out ? reinterpret_cast<uint32_t*>(out->rgba8) : ctx->rgba8.p) : nullptr;
-    ro.rgb = out->rgb ? (dev_out ? out->rgb : ctx->rgb.p) : nullptr;
-    if (keep_state) {
-        ro.final_t = ctx->final_t.p;
-        ro.n_contrib = ctx->n_contrib.p;
-    } else {
-        ro.final_t = out->final_t ? (dev_out ? out->final_t : ctx->final_t.p) : nullptr;
-        ro.n_contrib = out->n_contrib ? (dev_out ? out->n_contrib : ctx->n_contrib.p) : nullptr;
-    }
-
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    Frame& f = ctx->main;
+    rc = ensure_frame(ctx, f, a);
+    if (rc != GS_OK) return rc;
+    a.view = f.view.p;
+    a.out = raster_out(ctx, f, out);
     {
         const uint32_t slot = ctx->next_slot;
         ctx->next_slot = (slot + 1) % kViewSlots;
         GS_CK(cudaEventSynchronize(ctx->slot_done[slot]));
         std::memcpy(&ctx->h_views[slot], view, sizeof(ViewBlock));
-        GS_CK(cudaMemcpyAsync(ctx->view.p, &ctx->h_views[slot], sizeof(ViewBlock), cudaMemcpyHostToDevice, ctx->stream));
+        GS_CK(cudaMemcpyAsync(f.view.p, &ctx->h_views[slot], sizeof(ViewBlock), cudaMemcpyHostToDevice, ctx->stream));
         GS_CK(cudaEventRecord(ctx->slot_done[slot], ctx->stream));
     }
-    FrameArgs fa{scene, n, w, h, tiles_x, tiles_y, passes, max_instance, ro};
     const bool profile = (ctx->cfg.flags & GS_FLAG_PROFILE) != 0;
     const bool use_graph = !profile && (ctx->cfg.flags & GS_FLAG_NO_GRAPH) == 0;
     if (use_graph) {
-        GraphKey k{scene, n, w, h, ro.rgba8, ro.rgb, ro.final_t, ro.n_contrib, ctx->alloc_gen};
-        if (!ctx->exec || !(k == ctx->key)) {
-            if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
-            ctx->exec = nullptr;
-            cudaGraph_t g = nullptr;
-            GS_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_frame(ctx, fa, false);
-            cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
-            e = cudaGraphInstantiate(&ctx->exec, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) { ctx->exec = nullptr; return cuda_fail(ctx, e, "graph instantiate"); }
-            ctx->key = k;
-        }
-        ctx->sorted_buf = (int)(passes & 1u);
-        GS_CK(cudaGraphLaunch(ctx->exec, ctx->stream));
+        GraphKey k;
+        k.ptrs = {scene, a.out.rgba8, a.out.rgb, a.out.final_t, a.out.n_contrib};
+        k.dims = {a.n, a.w, a.h};
+        k.alloc_gen = ctx->alloc_gen;
+        rc = capture_and_launch(ctx, &ctx->exec, &ctx->key, k, {&f}, {a});
+        if (rc != GS_OK) return rc;
     } else {
-        enqueue_frame(ctx, fa, profile);
+        enqueue_frame(ctx, f, a, ctx->stream, profile);
     }
     GS_CK(cudaGetLastError());
-    ctx->last_scene = scene;
-    ctx->last_n = n;
-    ctx->width = w;
-    ctx->height = h;
-    ctx->tiles_x = tiles_x;
-    ctx->tiles_y = tiles_y;
-    ctx->passes = passes;
-    ctx->max_instance = max_instance;
-    ctx->have_frame = true;
+    remember(f, a);
     ctx->have_timing = false;
-    GS_CK(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
-    if (dev_out && keep_state) {
-        const size_t pix = (size_t)w * h;
-        if (out->final_t)
-            GS_CK(cudaMemcpyAsync(out->final_t, ctx->final_t.p, pix * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-        if (out->n_contrib)
-            GS_CK(cudaMemcpyAsync(out->n_contrib, ctx->n_contrib.p, pix * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-    }
-
-    if (!dev_out) {
-        const size_t pix = (size_t)w * h;
-        if (out->rgba8) GS_CK(cudaMemcpyAsync(out->rgba8, ctx->rgba8.p, pix * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        if (out->rgb) GS_CK(cudaMemcpyAsync(out->rgb, ctx->rgb.p, pix * 12, cudaMemcpyDeviceToHost, ctx->stream));
-        if (out->final_t) GS_CK(cudaMemcpyAsync(out->final_t, ctx->final_t.p, pix * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        if (out->n_contrib)
-            GS_CK(cudaMemcpyAsync(out->n_contrib, ctx->n_contrib.p, pix * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaMemcpyAsync(f.h_ctl, f.ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
+    rc = copy_outputs(ctx, f, out, ctx->stream);
+    if (rc != GS_OK) return rc;
+    if (out->location == GS_MEM_HOST) {
         GS_CK(cudaStreamSynchronize(ctx->stream));
         if (profile) {
             for (int p = 0; p < kPassCount; ++p) cudaEventElapsedTime(&ctx->pass_ms[p], ctx->ev[p], ctx->ev[p + 1]);
             ctx->have_timing = true;
         }
-        return status_to_code(ctx, ctx->h_ctl->status);
+        return status_to_code(ctx, f.h_ctl->status);
     }
+    return GS_OK;
+}
+
+int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!views || count == 0) return fail(ctx, GS_ERR_INVALID, "gs_forward_batch: no views");
+    const int32_t loc = views[0].out.location;
+    for (uint32_t i = 0; i < count; ++i)
+        if (views[i].out.location != loc || (loc != GS_MEM_HOST && loc != GS_MEM_DEVICE))
+            return fail(ctx, GS_ERR_INVALID, "gs_forward_batch: every view must use the same valid output location");
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    while (ctx->batch.size() < count) {
+        Frame* f = new Frame();
+        if (f->init(ctx->stream) != cudaSuccess) {
+            f->release();
+            delete f;
+            return fail(ctx, GS_ERR_OOM, "gs_forward_batch: frame allocation failed");
+        }
+        ctx->batch.push_back(f);
+        ++ctx->alloc_gen;
+    }
+    if (count > ctx->bviews_cap) {
+        GS_CK(cudaStreamSynchronize(ctx->stream));
+        if (ctx->h_bviews) cudaFreeHost(ctx->h_bviews);
+        ctx->h_bviews = nullptr;
+        ctx->bviews_cap = 0;
+        GS_CK(cudaMallocHost(&ctx->h_bviews, sizeof(ViewBlock) * count));
+        ctx->bviews_cap = count;
+        const void* before = ctx->d_bviews.p;
+        GS_CK(ctx->d_bviews.reserve(count));
+        if (before != ctx->d_bviews.p) ++ctx->alloc_gen;
+    }
+    std::vector<FrameArgs> args(count);
+    std::vector<Frame*> frames(ctx->batch.begin(), ctx->batch.begin() + count);
+    GraphKey k;
+    for (uint32_t i = 0; i < count; ++i) {
+        int rc = frame_args(ctx, views[i].scene, &views[i].view, &args[i]);
+        if (rc != GS_OK) return fail(ctx, rc, "gs_forward_batch: view " + std::to_string(i) + ": " + ctx->err);
+        rc = ensure_frame(ctx, *frames[i], args[i]);
+        if (rc != GS_OK) return rc;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        args[i].view = ctx->d_bviews.p + i;
+        args[i].out = raster_out(ctx, *frames[i], &views[i].out);
+        k.ptrs.insert(k.ptrs.end(), {views[i].scene, args[i].out.rgba8, args[i].out.rgb, args[i].out.final_t,
+                                     args[i].out.n_contrib});
+        k.dims.insert(k.dims.end(), {args[i].n, args[i].w, args[i].h});
+    }
+    k.alloc_gen = ctx->alloc_gen;
+    GS_CK(cudaEventSynchronize(ctx->bviews_done));
+    for (uint32_t i = 0; i < count; ++i) std::memcpy(&ctx->h_bviews[i], &views[i].view, sizeof(ViewBlock));
+    GS_CK(cudaMemcpyAsync(ctx->d_bviews.p, ctx->h_bviews, sizeof(ViewBlock) * count, cudaMemcpyHostToDevice, ctx->stream));
+    GS_CK(cudaEventRecord(ctx->bviews_done, ctx->stream));
+    int rc = capture_and_launch(ctx, &ctx->exec_batch, &ctx->key_batch, k, frames, args);
+    if (rc != GS_OK) return rc;
+    GS_CK(cudaGetLastError());
+    for (uint32_t i = 0; i < count; ++i) {
+        remember(*frames[i], args[i]);
+        GS_CK(cudaMemcpyAsync(frames[i]->h_ctl, frames[i]->ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+        rc = copy_outputs(ctx, *frames[i], &views[i].out, ctx->stream);
+        if (rc != GS_OK) return rc;
+    }
+    ctx->batch_count = count;
+    if (loc == GS_MEM_HOST) {
+        GS_CK(cudaStreamSynchronize(ctx->stream));
+        uint32_t status = 0;
+        for (uint32_t i = 0; i < count; ++i) status |= frames[i]->h_ctl->status;
+        return status_to_code(ctx, status);
+    }
+    return GS_OK;
+}
+
+static int fill_info(gs_ctx* ctx, const Frame& f, gs_frame_info* info) {
+    const FrameCtl& c = *f.h_ctl;
+    info->instance_count = c.instance_count;
+    info->sorted_count = c.sorted_count;
+    info->max_instance = f.max_instance;
+    info->visible = c.visible;
+    info->near_pass = c.near_pass;
+    info->tiles_x = f.tiles_x;
+    info->tiles_y = f.tiles_y;
+    info->status = c.status;
+    info->sort_passes = f.passes;
+    (void)ctx;
     return GS_OK;
 }
 
 int gs_get_frame_info(gs_ctx* ctx, gs_frame_info* info) {
     if (!ctx) return GS_ERR_INVALID;
     if (!info) return fail(ctx, GS_ERR_INVALID, "gs_get_frame_info: null info");
-    if (!ctx->have_frame) return fail(ctx, GS_ERR_STATE, "gs_get_frame_info: no frame rendered");
+    if (!ctx->main.valid) return fail(ctx, GS_ERR_STATE, "gs_get_frame_info: no frame rendered");
     GS_CK(cudaStreamSynchronize(ctx->stream));
     if (ctx->cfg.flags & GS_FLAG_PROFILE && !ctx->have_timing) {
         for (int p = 0; p < kPassCount; ++p) cudaEventElapsedTime(&ctx->pass_ms[p], ctx->ev[p], ctx->ev[p + 1]);
         ctx->have_timing = true;
     }
-    const FrameCtl& c = *ctx->h_ctl;
-    info->instance_count = c.instance_count;
-    info->sorted_count = c.sorted_count;
-    info->max_instance = ctx->max_instance;
-    info->visible = c.visible;
-    info->near_pass = c.near_pass;
-    info->tiles_x = ctx->tiles_x;
-    info->tiles_y = ctx->tiles_y;
-    info->status = c.status;
-    info->sort_passes = ctx->passes;
-    return GS_OK;
+    return fill_info(ctx, ctx->main, info);
+}
+
+int gs_get_batch_frame_info(gs_ctx* ctx, uint32_t index, gs_frame_info* info) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!info) return fail(ctx, GS_ERR_INVALID, "gs_get_batch_frame_info: null info");
+    if (index >= ctx->batch_count || !ctx->batch[index]->valid)
+        return fail(ctx, GS_ERR_STATE, "gs_get_batch_frame_info: no such view in the last batch");
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    return fill_info(ctx, *ctx->batch[index], info);
 }
 
 int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg) {
     if (!ctx) return GS_ERR_INVALID;
     if (!dbg) return fail(ctx, GS_ERR_INVALID, "gs_get_debug: null argument");
-    if (!ctx->have_frame) return fail(ctx, GS_ERR_STATE, "gs_get_debug: no frame rendered");
+    Frame& f = ctx->main;
+    if (!f.valid) return fail(ctx, GS_ERR_STATE, "gs_get_debug: no frame rendered");
     GS_CK(cudaStreamSynchronize(ctx->stream));
-    const uint32_t n = ctx->last_n;
-    if (dbg->tiles_touched) GS_CK(cudaMemcpy(dbg->tiles_touched, ctx->counts.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
-    if (dbg->meta) GS_CK(cudaMemcpy(dbg->meta, ctx->meta.p, (size_t)n * 16, cudaMemcpyDeviceToHost));
+    const uint32_t n = f.n;
+    if (dbg->tiles_touched) GS_CK(cudaMemcpy(dbg->tiles_touched, f.counts.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    if (dbg->meta) GS_CK(cudaMemcpy(dbg->meta, f.meta.p, (size_t)n * 16, cudaMemcpyDeviceToHost));
     if (dbg->conic_opacity || dbg->pixel || dbg->color) {
         std::vector<float> rec((size_t)n * kRecFloat4 * 4);
-        if (n) GS_CK(cudaMemcpy(rec.data(), ctx->rec.p, rec.size() * 4, cudaMemcpyDeviceToHost));
+        if (n) GS_CK(cudaMemcpy(rec.data(), f.rec.p, rec.size() * 4, cudaMemcpyDeviceToHost));
         for (size_t g = 0; g < n; ++g) {
             const float* r = rec.data() + g * 12;
             if (dbg->pixel) { dbg->pixel[2 * g] = r[0]; dbg->pixel[2 * g + 1] = r[1]; }
@@ -533,13 +721,13 @@ int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg) {
             }
         }
     }
-    if (dbg->offsets) GS_CK(cudaMemcpy(dbg->offsets, ctx->offsets.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
-    const uint32_t sorted = ctx->h_ctl->sorted_count;
+    if (dbg->offsets) GS_CK(cudaMemcpy(dbg->offsets, f.offsets.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+    const uint32_t sorted = f.h_ctl->sorted_count;
     const size_t kc = std::min<uint64_t>(sorted, dbg->capacity);
-    if (dbg->keys && kc) GS_CK(cudaMemcpy(dbg->keys, ctx->keys[ctx->sorted_buf].p, kc * 4, cudaMemcpyDeviceToHost));
-    if (dbg->vals && kc) GS_CK(cudaMemcpy(dbg->vals, ctx->vals[ctx->sorted_buf].p, kc * 4, cudaMemcpyDeviceToHost));
+    if (dbg->keys && kc) GS_CK(cudaMemcpy(dbg->keys, f.keys[f.sorted_buf].p, kc * 4, cudaMemcpyDeviceToHost));
+    if (dbg->vals && kc) GS_CK(cudaMemcpy(dbg->vals, f.vals[f.sorted_buf].p, kc * 4, cudaMemcpyDeviceToHost));
     if (dbg->ranges)
-        GS_CK(cudaMemcpy(dbg->ranges, ctx->ranges.p, (size_t)ctx->tiles_x * ctx->tiles_y * 8, cudaMemcpyDeviceToHost));
+        GS_CK(cudaMemcpy(dbg->ranges, f.ranges.p, (size_t)f.tiles_x * f.tiles_y * 8, cudaMemcpyDeviceToHost));
     return GS_OK;
 }
 
@@ -547,7 +735,7 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
     if (!ctx) return GS_ERR_INVALID;
     if (!rows || !n_rows || max_rows < 0) return fail(ctx, GS_ERR_INVALID, "gs_get_timings: bad argument");
     if (!(ctx->cfg.flags & GS_FLAG_PROFILE)) return fail(ctx, GS_ERR_STATE, "gs_get_timings: context not profiling");
-    if (!ctx->have_frame) return fail(ctx, GS_ERR_STATE, "gs_get_timings: no frame rendered");
+    if (!ctx->main.valid) return fail(ctx, GS_ERR_STATE, "gs_get_timings: no frame rendered");
     if (!ctx->have_timing) {
         GS_CK(cudaStreamSynchronize(ctx->stream));
         for (int p = 0; p < kPassCount; ++p) cudaEventElapsedTime(&ctx->pass_ms[p], ctx->ev[p], ctx->ev[p + 1]);
@@ -569,32 +757,23 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
     return GS_OK;
 }
 
-int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location) {
-    if (!ctx) return GS_ERR_INVALID;
-    if (!scene || !dl_drgb || !grad_packed || (location != GS_MEM_HOST && location != GS_MEM_DEVICE))
-        return fail(ctx, GS_ERR_INVALID, "gs_backward: bad argument");
-    if (!(ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE))
-        return fail(ctx, GS_ERR_STATE, "gs_backward: context was created without GS_FLAG_DIFFERENTIABLE");
-    if (!ctx->have_frame || ctx->last_scene != scene || ctx->last_n != scene->n)
-        return fail(ctx, GS_ERR_STATE, "gs_backward: the last gs_forward on this context was not on this scene");
-    GS_CK(cudaSetDevice(ctx->cfg.device));
-    const uint32_t n = scene->n, w = ctx->width, h = ctx->height;
-    const size_t pix = (size_t)w * h;
-    GS_CK(ctx->grad2d.reserve((size_t)n * 9));
-    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
-    const float* dl = dl_drgb;
-    if (location == GS_MEM_HOST) {
-        GS_CK(ctx->dl_stage.reserve(pix * 3));
-        GS_CK(cudaMemcpyAsync(ctx->dl_stage.p, dl_drgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
-        dl = ctx->dl_stage.p;
-    }
-    if (n) GS_CK(cudaMemsetAsync(ctx->grad2d.p, 0, (size_t)n * 9 * sizeof(float), ctx->stream));
-    launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, ctx->ranges.p, ctx->vals[ctx->sorted_buf].p,
-                           ctx->rec.p, n, ctx->ctl.p, w, h, ctx->tiles_x, ctx->tiles_y, ctx->final_t.p,
-                           ctx->n_contrib.p, dl, ctx->grad2d.p, ctx->stream);
-    launch_preprocess_backward(scene->rows, scene->stride, n, ctx->view.p, ctx->counts.p, ctx->grad2d.p,
-                               ctx->grows.p, ctx->stream);
+// ---- backward --------------------------------------------------------------------------------------
+// Raster backward of frame f into f.grad2d, then the preprocess backward into ctx->grows.
+static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, bool accumulate,
+                            cudaStream_t s) {
+    GS_CK(f.grad2d.reserve((size_t)scene->n * 9));
+    if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
+    launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[f.sorted_buf].p, f.rec.p,
+                           scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
+                           f.grad2d.p, s);
+    launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p,
+                               ctx->grows.p, accumulate, s);
     GS_CK(cudaGetLastError());
+    return GS_OK;
+}
+
+static int finish_grads(gs_ctx* ctx, const gs_scene* scene, float* grad_packed, int32_t location) {
+    const uint32_t n = scene->n;
     if (location == GS_MEM_DEVICE) {
         launch_rows_to_pack(ctx->grows.p, n, scene->stride, grad_packed, ctx->stream);
         GS_CK(cudaGetLastError());
@@ -606,6 +785,72 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
     if (n) GS_CK(cudaMemcpyAsync(grad_packed, ctx->grad_stage.p, (size_t)n * kRows * 4, cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
     return GS_OK;
+}
+
+int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!scene || !dl_drgb || !grad_packed || (location != GS_MEM_HOST && location != GS_MEM_DEVICE))
+        return fail(ctx, GS_ERR_INVALID, "gs_backward: bad argument");
+    if (!(ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE))
+        return fail(ctx, GS_ERR_STATE, "gs_backward: context was created without GS_FLAG_DIFFERENTIABLE");
+    Frame& f = ctx->main;
+    if (!f.valid || f.scene != scene || f.n != scene->n)
+        return fail(ctx, GS_ERR_STATE, "gs_backward: the last gs_forward on this context was not on this scene");
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
+    const float* dl = dl_drgb;
+    if (location == GS_MEM_HOST) {
+        const size_t pix = (size_t)f.width * f.height;
+        GS_CK(f.dl_stage.reserve(pix * 3));
+        GS_CK(cudaMemcpyAsync(f.dl_stage.p, dl_drgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
+        dl = f.dl_stage.p;
+    }
+    const int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream);
+    if (rc != GS_OK) return rc;
+    return finish_grads(ctx, scene, grad_packed, location);
+}
+
+int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
+                      float* grad_packed, int32_t location) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!scene || !dl_drgb || !grad_packed || count == 0 || (location != GS_MEM_HOST && location != GS_MEM_DEVICE))
+        return fail(ctx, GS_ERR_INVALID, "gs_backward_batch: bad argument");
+    if (!(ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE))
+        return fail(ctx, GS_ERR_STATE, "gs_backward_batch: context was created without GS_FLAG_DIFFERENTIABLE");
+    if (count > ctx->batch_count) return fail(ctx, GS_ERR_STATE, "gs_backward_batch: more views than the last batch");
+    for (uint32_t i = 0; i < count; ++i) {
+        const Frame& f = *ctx->batch[i];
+        if (!dl_drgb[i]) return fail(ctx, GS_ERR_INVALID, "gs_backward_batch: null dL/drgb");
+        if (!f.valid || f.scene != scene || f.n != scene->n)
+            return fail(ctx, GS_ERR_STATE, "gs_backward_batch: view " + std::to_string(i) + " of the last batch is not of this scene");
+    }
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
+    GS_CK(cudaMemsetAsync(ctx->grows.p, 0, (size_t)scene->stride * kRows * sizeof(float), ctx->stream));
+    std::vector<const float*> dls(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        Frame& f = *ctx->batch[i];
+        dls[i] = dl_drgb[i];
+        if (location == GS_MEM_HOST) {
+            const size_t pix = (size_t)f.width * f.height;
+            GS_CK(f.dl_stage.reserve(pix * 3));
+            GS_CK(cudaMemcpyAsync(f.dl_stage.p, dl_drgb[i], pix * 12, cudaMemcpyHostToDevice, ctx->stream));
+            dls[i] = f.dl_stage.p;
+        }
+    }
+    // views run concurrently on the side streams; their Gaussian gradients meet in grows by atomics
+    GS_CK(cudaEventRecord(ctx->fork, ctx->stream));
+    const int used = (int)std::min<uint32_t>(count, kSideStreams);
+    for (int s = 0; s < used; ++s) GS_CK(cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0));
+    for (uint32_t i = 0; i < count; ++i) {
+        const int rc = enqueue_backward(ctx, *ctx->batch[i], scene, dls[i], true, ctx->side[i % used]);
+        if (rc != GS_OK) return rc;
+    }
+    for (int s = 0; s < used; ++s) {
+        GS_CK(cudaEventRecord(ctx->join[s], ctx->side[s]));
+        GS_CK(cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0));
+    }
+    return finish_grads(ctx, scene, grad_packed, location);
 }
 
 int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t width, uint32_t height,
@@ -638,9 +883,74 @@ int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t
         double sums[2] = {0.0, 0.0};
         GS_CK(cudaMemcpyAsync(sums, ctx->loss_sums.p, sizeof(sums), cudaMemcpyDeviceToHost, ctx->stream));
         GS_CK(cudaStreamSynchronize(ctx->stream));
-        const double count = 3.0 * (double)pix;
-        if (loss) *loss = sums[1] / count + (double)lambda * (1.0 - sums[0] / count);
+        const double cnt = 3.0 * (double)pix;
+        if (loss) *loss = sums[1] / cnt + (double)lambda * (1.0 - sums[0] / cnt);
     }
+    return GS_OK;
+}
+
+// ---- autotuner -------------------------------------------------------------------------------------
+int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
+                uint32_t iters, gs_config* best, float* best_ms) {
+    if (!packed || !views || n_views == 0 || !best) return GS_ERR_INVALID;
+    gs_config b;
+    gs_config_default(&b);
+    if (base) b = *base;
+    const uint32_t tiles[] = {8, 16, 32};
+    const uint32_t digits[] = {4, 8};
+    const uint32_t batches[] = {32, 64, 128, 256};
+    float best_t = 3.0e38f;
+    gs_config best_c = b;
+    for (uint32_t t : tiles)
+        for (uint32_t d : digits)
+            for (uint32_t r : batches) {
+                gs_config c = b;
+                c.tile_size = t;
+                c.digit_bits = d;
+                c.raster_batch = r;
+                c.flags &= ~(GS_FLAG_PROFILE | GS_FLAG_DIFFERENTIABLE);
+                gs_ctx* ctx = nullptr;
+                if (gs_ctx_create(&c, &ctx) != GS_OK) return GS_ERR_CUDA;
+                gs_scene* sc = nullptr;
+                int rc = gs_scene_upload(ctx, packed, count, GS_MEM_HOST, &sc);
+                std::vector<gs_batch_view> bv(n_views);
+                std::vector<uint32_t*> imgs(n_views, nullptr);
+                for (uint32_t i = 0; rc == GS_OK && i < n_views; ++i) {
+                    const size_t pix = (size_t)views[i].texture_size[0] * (size_t)views[i].texture_size[1];
+                    if (cudaMalloc(&imgs[i], pix * 4) != cudaSuccess) rc = GS_ERR_OOM;
+                    bv[i].scene = sc;
+                    bv[i].view = views[i];
+                    bv[i].out = gs_image{GS_MEM_DEVICE, reinterpret_cast<uint8_t*>(imgs[i]), nullptr, nullptr, nullptr};
+                }
+                float ms = 0.0f;
+                if (rc == GS_OK) {
+                    for (int w = 0; w < 2 && rc == GS_OK; ++w) rc = gs_forward_batch(ctx, bv.data(), n_views);
+                    cudaEvent_t e0, e1;
+                    cudaEventCreate(&e0);
+                    cudaEventCreate(&e1);
+                    cudaEventRecord(e0, ctx->stream);
+                    for (uint32_t k = 0; k < std::max(iters, 1u) && rc == GS_OK; ++k) rc = gs_forward_batch(ctx, bv.data(), n_views);
+                    cudaEventRecord(e1, ctx->stream);
+                    cudaEventSynchronize(e1);
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    ms /= (float)std::max(iters, 1u);
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    if (rc == GS_OK) rc = gs_ctx_synchronize(ctx);
+                }
+                for (uint32_t* p : imgs)
+                    if (p) cudaFree(p);
+                if (sc) gs_scene_destroy(sc);
+                gs_ctx_destroy(ctx);
+                if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return rc;
+                if (ms < best_t) {
+                    best_t = ms;
+                    best_c = c;
+                }
+            }
+    best_c.flags = b.flags;
+    *best = best_c;
+    if (best_ms) *best_ms = best_t;
     return GS_OK;
 }
 
@@ -684,12 +994,9 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
     const cudaMemcpyKind kout = location == GS_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     GS_CK(cudaMemcpyAsync(keys, kb[cur], (size_t)n * 4, kout, ctx->stream));
     GS_CK(cudaMemcpyAsync(vals, vb[cur], (size_t)n * 4, kout, ctx->stream));
-    uint32_t status = 0;
-    GS_CK(cudaMemcpyAsync(ctx->h_ctl, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaMemcpyAsync(ctx->h_aux, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
-    status = ctx->h_ctl->status;
-    ctx->have_frame = false;  // the readback block now holds the sort's counters
-    return status_to_code(ctx, status);
+    return status_to_code(ctx, ctx->h_aux->status);
 }
 
 int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, int32_t location) {
@@ -714,12 +1021,11 @@ int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, 
     const cudaMemcpyKind kout = location == GS_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     if (n) GS_CK(cudaMemcpyAsync(data, d, (size_t)n * 4, kout, ctx->stream));
     uint32_t tot = 0;
-    GS_CK(cudaMemcpyAsync(ctx->h_ctl, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaMemcpyAsync(ctx->h_aux, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaMemcpyAsync(&tot, d + n, 4, cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
     if (total) *total = tot;
-    ctx->have_frame = false;
-    return status_to_code(ctx, ctx->h_ctl->status);
+    return status_to_code(ctx, ctx->h_aux->status);
 }
 
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {

@@ -213,14 +213,18 @@ __global__ void __launch_bounds__(256) k_preprocess_backward(const float* __rest
                                                              uint32_t n, const ViewBlock* __restrict__ vb,
                                                              const uint32_t* __restrict__ counts,
                                                              const float* __restrict__ grad2d,
-                                                             float* __restrict__ grows) {
+                                                             float* __restrict__ grows, int accumulate) {
     __shared__ ViewBlock sv;
     if (threadIdx.x < 44) reinterpret_cast<uint32_t*>(&sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(vb)[threadIdx.x];
     __syncthreads();
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
     auto R_ = [&](int row) { return __ldg(rows + (size_t)row * stride + g); };
-    auto W_ = [&](int row, float v) { grows[(size_t)row * stride + g] = v; };
+    // accumulate: several views of one scene add into the same rows (FP32 atomics)
+    auto W_ = [&](int row, float v) {
+        float* dst = grows + (size_t)row * stride + g;
+        if (accumulate) atomicAdd(dst, v); else *dst = v;
+    };
     if (counts[g] == 0u) {
         for (int r = 0; r < kRows; ++r) W_(r, 0.0f);
         return;
@@ -424,9 +428,11 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
 }
 
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* grows, cudaStream_t s) {
+                                const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
+                                cudaStream_t s) {
     if (n == 0) return;
-    k_preprocess_backward<<<(n + 255u) / 256u, 256, 0, s>>>(rows, stride, n, view, counts, grad2d, grows);
+    k_preprocess_backward<<<(n + 255u) / 256u, 256, 0, s>>>(rows, stride, n, view, counts, grad2d, grows,
+                                                            accumulate ? 1 : 0);
 }
 
 }  // namespace gs

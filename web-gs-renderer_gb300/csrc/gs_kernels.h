@@ -72,8 +72,10 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
                             const float* dl_drgb, float* grad2d, cudaStream_t s);
 // grad2d -> dL/d(attribute rows), one thread per Gaussian, rows laid out like the scene.
+// accumulate: add into grows with FP32 atomics (several views of one scene) instead of storing.
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* grows, cudaStream_t s);
+                                const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
+                                cudaStream_t s);
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------
 size_t loss_scratch_floats(uint32_t width, uint32_t height);

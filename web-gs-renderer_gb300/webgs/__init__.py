@@ -222,6 +222,37 @@ class Context:
         self._ck(library().gs_backward(self.handle, scene.handle, _ptr(dl), _ptr(g), GS_MEM_HOST))
         return g
 
+    def forward_batch(self, items: list, rgba8: bool = True, rgb: bool = False) -> list[dict]:
+        """Renders [(scene, view), ...] in one batched launch into new host arrays."""
+        arr = (_abi.BatchView * len(items))()
+        outs = []
+        for i, (scene, view) in enumerate(items):
+            w, h = int(view.texture_size[0]), int(view.texture_size[1])
+            res = {}
+            if rgba8:
+                res["rgba8"] = np.empty((h, w, 4), dtype=np.uint8)
+            if rgb:
+                res["rgb"] = np.empty((h, w, 3), dtype=np.float32)
+            arr[i].scene = scene.handle
+            arr[i].view = view
+            arr[i].out = Image(GS_MEM_HOST, _ptr(res.get("rgba8")), _ptr(res.get("rgb")), None, None)
+            outs.append(res)
+        self._ck(library().gs_forward_batch(self.handle, arr, len(items)))
+        return outs
+
+    def batch_frame_info(self, index: int) -> dict:
+        fi = FrameInfo()
+        self._ck(library().gs_get_batch_frame_info(self.handle, index, C.byref(fi)))
+        return {k: getattr(fi, k) for k, _ in FrameInfo._fields_}
+
+    def backward_batch(self, scene: Scene, dl_drgbs: list) -> np.ndarray:
+        """Summed gradient of views 0..len-1 of the last batch (all of `scene`)."""
+        dls = [np.ascontiguousarray(d, dtype=np.float32) for d in dl_drgbs]
+        ptrs = (C.c_void_p * len(dls))(*[_ptr(d) for d in dls])
+        g = np.zeros(scene.count * FLOATS_PER_GAUSSIAN, np.float32)
+        self._ck(library().gs_backward_batch(self.handle, scene.handle, ptrs, len(dls), _ptr(g), GS_MEM_HOST))
+        return g
+
     def loss(self, rgb: np.ndarray, target: np.ndarray, lam: float = 0.2) -> tuple[float, np.ndarray]:
         """L1 + lam * (1 - SSIM) of an H x W x 3 image against a target, and dL/drgb."""
         x = np.ascontiguousarray(rgb, dtype=np.float32)
@@ -261,6 +292,21 @@ def _forward_tracking(fn):
 
 Context.forward = _forward_tracking(Context.forward)
 Context.forward_device = _forward_tracking(Context.forward_device)
+
+
+def autotune(packed: np.ndarray, count: int, views: list, iters: int = 5, device: int = 0,
+             max_instance_factor: int = 64) -> tuple[dict, float]:
+    """Sweeps tile size x radix digit width x raster batch depth for a batch of views of one scene
+    (gs_autotune); returns the fastest configuration and its ms per batch."""
+    base = Config()
+    library().gs_config_default(C.byref(base))
+    base.device, base.max_instance_factor = device, max_instance_factor
+    arr = (View * len(views))(*views)
+    best, ms = Config(), C.c_float()
+    p = np.ascontiguousarray(packed, dtype=np.float32)
+    _check(library().gs_autotune(C.byref(base), _ptr(p), count, arr, len(views), iters, C.byref(best), C.byref(ms)),
+           None, "gs_autotune")
+    return {"tile_size": best.tile_size, "digit_bits": best.digit_bits, "raster_batch": best.raster_batch}, ms.value
 
 
 # ---- Camera (src/renderer/camera.js) -------------------------------------------------------------

@@ -77,6 +77,10 @@ class Timing(C.Structure):
     _fields_ = [("label", C.c_char * 24), ("ms", C.c_float)]
 
 
+class BatchView(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("view", View), ("out", Image)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/gs.h
 SIGNATURES = [
     ("gs_version", C.c_char_p, []),
@@ -92,6 +96,12 @@ SIGNATURES = [
     ("gs_scene_count", C.c_uint32, [C.c_void_p]),
     ("gs_forward", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(View), C.POINTER(Image)]),
     ("gs_get_frame_info", C.c_int, [C.c_void_p, C.POINTER(FrameInfo)]),
+    ("gs_forward_batch", C.c_int, [C.c_void_p, C.POINTER(BatchView), C.c_uint32]),
+    ("gs_get_batch_frame_info", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(FrameInfo)]),
+    ("gs_backward_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_void_p,
+                                    C.c_int32]),
+    ("gs_autotune", C.c_int, [C.POINTER(Config), C.c_void_p, C.c_uint32, C.POINTER(View), C.c_uint32, C.c_uint32,
+                              C.POINTER(Config), C.POINTER(C.c_float)]),
     ("gs_get_debug", C.c_int, [C.c_void_p, C.POINTER(Debug)]),
     ("gs_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
     ("gs_loss_l1_ssim", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
