@@ -415,10 +415,6 @@ def main():
         run_ours(args, rank, world, local_rank)
 
 
-if __name__ == "__main__":
-    main()
-
-
 def _timed(stream, fn, steps, warmup):
     import torch
 
@@ -481,6 +477,38 @@ def batched_forward(steps, warmup, local_rank) -> dict:
                       "batched_ms_per_view": round(ms_batch / len(cams), 4),
                       "plain_Mpix_s": round(pix / ms_plain / 1e3, 1), "batched_Mpix_s": round(pix / ms_batch / 1e3, 1),
                       "batched_over_plain": round(ms_plain / ms_batch, 3)}
+        if label == "default":
+            # end to end: every view's rgba8 image lands in pinned host memory; plain = one synchronous
+            # gs_forward per view (one Renderer.execute() per view), batched = one gs_forward_batch
+            hosts = [torch.empty(c.width * c.height * 4, dtype=torch.uint8, pin_memory=True) for _, c in cams]
+            harr = (_abi.BatchView * len(cams))()
+            for k, ((si, c), v) in enumerate(zip(cams, views)):
+                harr[k].scene = scs[si].handle
+                harr[k].view = v
+                harr[k].out = _abi.Image(webgs.GS_MEM_HOST, hosts[k].data_ptr(), None, None, None)
+
+            def plain_e2e():
+                for k, (si, _) in enumerate(cams):
+                    img = _abi.Image(webgs.GS_MEM_HOST, hosts[k].data_ptr(), None, None, None)
+                    ctx._ck(lib.gs_forward(ctx.handle, scs[si].handle, C.byref(views[k]), C.byref(img)))
+
+            def batch_e2e():
+                ctx._ck(lib.gs_forward_batch(ctx.handle, harr, len(cams)))
+
+            for fn in (plain_e2e, batch_e2e):
+                fn(); fn()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                plain_e2e()
+            t_plain = (time.perf_counter() - t0) / steps
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                batch_e2e()
+            t_batch = (time.perf_counter() - t0) / steps
+            res[label]["e2e"] = {"plain_ms_per_view": round(t_plain * 1e3 / len(cams), 4),
+                                 "batched_ms_per_view": round(t_batch * 1e3 / len(cams), 4),
+                                 "batched_over_plain": round(t_plain / t_batch, 3),
+                                 "d2h_bytes_per_batch": 4 * pix}
         for s in scs:
             s.close()
         ctx.close()
@@ -551,3 +579,7 @@ def batched_fwd_bwd(steps, warmup, local_rank) -> dict:
     return {"workload": "3M Gaussians (128 clusters, 40^3 box, seed 6), 8 x 1920x1080, L1 + 0.2(1-SSIM)",
             "sequential_ms_per_view": round(ms_seq / len(views), 4), "batched_ms_per_view": round(ms_bat / len(views), 4),
             "batched_over_sequential": round(ms_seq / ms_bat, 3)}
+
+
+if __name__ == "__main__":
+    main()

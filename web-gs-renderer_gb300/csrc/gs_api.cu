@@ -47,7 +47,7 @@ template <class T> struct DevBuf {
 uint32_t bitlen(uint32_t v) { return v == 0 ? 0u : 32u - (uint32_t)__builtin_clz(v); }
 
 constexpr int kViewSlots = 16;
-constexpr int kSideStreams = 4;
+constexpr int kSideStreams = 16;
 enum Pass { kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
 const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile ranges", "raster"};
 
@@ -151,6 +151,8 @@ struct gs_ctx {
     cudaEvent_t ev[kPassCount + 1] = {};
     float pass_ms[kPassCount] = {};
     bool have_timing = false;
+    cudaEvent_t bev[3] = {};  // raster backward / preprocess backward of the last gs_backward
+    bool have_bwd = false;
 };
 
 namespace {
@@ -411,6 +413,7 @@ int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
     }
     cudaMemsetAsync(ctx->aux_ctl.p, 0, sizeof(FrameCtl), ctx->stream);
     for (auto& e : ctx->ev) cudaEventCreate(&e);
+    for (auto& e : ctx->bev) cudaEventCreate(&e);
     for (auto& e : ctx->slot_done) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         gs_ctx_destroy(ctx);
@@ -427,6 +430,8 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     if (ctx->exec_batch) cudaGraphExecDestroy(ctx->exec_batch);
     for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->bev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->slot_done)
         if (e) cudaEventDestroy(e);
@@ -572,6 +577,7 @@ int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs
     GS_CK(cudaGetLastError());
     remember(f, a);
     ctx->have_timing = false;
+    ctx->have_bwd = false;
     GS_CK(cudaMemcpyAsync(f.h_ctl, f.ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
     rc = copy_outputs(ctx, f, out, ctx->stream);
     if (rc != GS_OK) return rc;
@@ -753,6 +759,14 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
         rows[k].ms = total;
         ++k;
     }
+    if (ctx->have_bwd) {  // the last gs_backward, after the forward rows
+        GS_CK(cudaStreamSynchronize(ctx->stream));
+        const char* labels[2] = {"raster backward", "preprocess backward"};
+        for (int p = 0; p < 2 && k < max_rows; ++p, ++k) {
+            std::snprintf(rows[k].label, sizeof(rows[k].label), "%s", labels[p]);
+            cudaEventElapsedTime(&rows[k].ms, ctx->bev[p], ctx->bev[p + 1]);
+        }
+    }
     *n_rows = k;
     return GS_OK;
 }
@@ -760,14 +774,17 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 // ---- backward --------------------------------------------------------------------------------------
 // Raster backward of frame f into f.grad2d, then the preprocess backward into ctx->grows.
 static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, bool accumulate,
-                            cudaStream_t s) {
+                            cudaStream_t s, cudaEvent_t* ev = nullptr) {
     GS_CK(f.grad2d.reserve((size_t)scene->n * 9));
     if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
+    if (ev) cudaEventRecord(ev[0], s);
     launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[f.sorted_buf].p, f.rec.p,
                            scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
                            f.grad2d.p, s);
+    if (ev) cudaEventRecord(ev[1], s);
     launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p,
                                ctx->grows.p, accumulate, s);
+    if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
     return GS_OK;
 }
@@ -805,8 +822,10 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
         GS_CK(cudaMemcpyAsync(f.dl_stage.p, dl_drgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
         dl = f.dl_stage.p;
     }
-    const int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream);
+    const bool profile = (ctx->cfg.flags & GS_FLAG_PROFILE) != 0;
+    const int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream, profile ? ctx->bev : nullptr);
     if (rc != GS_OK) return rc;
+    ctx->have_bwd = profile;
     return finish_grads(ctx, scene, grad_packed, location);
 }
 
@@ -862,7 +881,7 @@ int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t
     GS_CK(cudaSetDevice(ctx->cfg.device));
     const size_t pix = (size_t)width * height;
     GS_CK(ctx->loss_scratch.reserve(loss_scratch_floats(width, height)));
-    GS_CK(ctx->loss_sums.reserve(2));
+    GS_CK(ctx->loss_sums.reserve(loss_sum_doubles(width, height)));
     const float* x = rgb;
     const float* y = target;
     float* dl = dl_drgb;

@@ -62,6 +62,34 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// Warp reduce-scatter of eight values: after it, each lane holds the warp total of value
+// (lane >> 2) & 7. Halving stages: xor 16 splits the values 0-3 | 4-7 between the half-warps, xor 8
+// splits each half again, xor 4 once more (4 + 2 + 1 shuffles), then xor 2 and xor 1 finish the
+// sums: 9 shuffles instead of 40 for eight separate reductions.
+__device__ __forceinline__ float warp_reduce_scatter8(const float v[8]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool b4 = lane & 16u, b3 = lane & 8u, b2 = lane & 4u;
+    float w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float send = b4 ? v[k] : v[k + 4];
+        const float keep = b4 ? v[k + 4] : v[k];
+        w[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    float u[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float send = b3 ? w[k] : w[k + 2];
+        const float keep = b3 ? w[k + 2] : w[k];
+        u[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    const float send = b2 ? u[0] : u[1];
+    float t = (b2 ? u[1] : u[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    return t;
+}
+
 template <int TILE, int BATCH>
 __global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t* __restrict__ ranges,
                                                                  const uint32_t* __restrict__ vals,
@@ -191,15 +219,14 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t*
                     }
                 }
                 if (__any_sync(0xffffffffu, contrib)) {
-                    g_px = warp_sum(g_px); g_py = warp_sum(g_py); g_a = warp_sum(g_a); g_b = warp_sum(g_b);
-                    g_c = warp_sum(g_c); g_o = warp_sum(g_o); g_r = warp_sum(g_r); g_g = warp_sum(g_g);
-                    g_bl = warp_sum(g_bl);
+                    const float v8[8] = {g_px, g_py, g_a, g_b, g_c, g_o, g_r, g_g};
+                    const float mine = warp_reduce_scatter8(v8);  // total of value (lane >> 2) & 7
+                    const float blue = warp_sum(g_bl);
                     const uint32_t gi = s_g[j];
-                    if (lane == 0 && gi < n) {
+                    if (gi < n) {
                         float* dst = grad2d + (size_t)9 * gi;
-                        atomicAdd(dst + 0, g_px); atomicAdd(dst + 1, g_py); atomicAdd(dst + 2, g_a);
-                        atomicAdd(dst + 3, g_b); atomicAdd(dst + 4, g_c); atomicAdd(dst + 5, g_o);
-                        atomicAdd(dst + 6, g_r); atomicAdd(dst + 7, g_g); atomicAdd(dst + 8, g_bl);
+                        if ((lane & 3u) == 0u) atomicAdd(dst + ((lane >> 2) & 7u), mine);
+                        if (lane == 2u) atomicAdd(dst + 8, blue);
                     }
                 }
             }

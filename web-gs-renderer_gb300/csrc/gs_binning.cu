@@ -282,21 +282,23 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     const uint32_t n = n_dev ? *n_dev : n_host;
     const uint32_t nparts = (n + kSortPartition - 1u) / kSortPartition;
 
-    // global digit bases of this pass: exclusive scan of the histogram
-    {
-        const uint32_t h = tid < RADIX ? hist[tid] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan<kSortThreads>(h, s_warp, &tot);
-        if (tid < RADIX) s_gbase[tid] = ex;
-    }
     if (tid == 0) s_seq = ctl->seq + slot;
+    bool have_bases = false;
 
     while (true) {
         __syncthreads();
         if (tid == 0) s_part = atomicAdd(&ctl->tickets[slot], 1u);
         __syncthreads();
         const uint32_t part = s_part, seq = s_seq;
-        if (part >= nparts) break;
+        if (part >= nparts) break;  // CTAs left without a partition exit before any other work
+        if (!have_bases) {
+            // global digit bases of this pass: exclusive scan of the histogram
+            const uint32_t h = tid < RADIX ? hist[tid] : 0u;
+            uint32_t tot;
+            const uint32_t ex = block_exclusive_scan<kSortThreads>(h, s_warp, &tot);
+            if (tid < RADIX) s_gbase[tid] = ex;
+            have_bases = true;
+        }
         const uint32_t base = part * kSortPartition;
         const uint32_t valid_n = min(kSortPartition, n - base);
 

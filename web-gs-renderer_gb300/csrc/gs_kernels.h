@@ -79,7 +79,9 @@ void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, 
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------
 size_t loss_scratch_floats(uint32_t width, uint32_t height);
-// sums[0] = sum of the SSIM map, sums[1] = sum |x - y| (both over W*H*3); dl may be null.
+size_t loss_sum_doubles(uint32_t width, uint32_t height);
+// sums (loss_sum_doubles entries): [0] = sum of the SSIM map, [1] = sum |x - y| (both over W*H*3),
+// then per-block partials; dl may be null.
 void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_t height, float lambda,
                          float* scratch, double* sums, float* dl, cudaStream_t s);
 

@@ -93,9 +93,41 @@ __global__ void k_moments_v(const float* __restrict__ hm, const float* __restric
             a += __shfl_xor_sync(0xffffffffu, a, k);
             b += __shfl_xor_sync(0xffffffffu, b, k);
         }
+        if (lane == 0) {  // one partial per block; k_reduce_sums adds them (no contended atomics)
+            const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            sums[2 * blk] = (double)a;
+            sums[2 * blk + 1] = (double)b;
+        }
+    }
+}
+
+// sums[0..1] = column sums of the per-block partials that follow them
+__global__ void k_reduce_sums(double* __restrict__ sums, size_t blocks) {
+    __shared__ double red[2][32];
+    double a = 0.0, b = 0.0;
+    const double* part = sums + 2;
+    for (size_t i = threadIdx.x; i < blocks; i += blockDim.x) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    for (int k = 16; k > 0; k >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, k);
+        b += __shfl_xor_sync(0xffffffffu, b, k);
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0) { red[0][warp] = a; red[1][warp] = b; }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        a = lane < nw ? red[0][lane] : 0.0;
+        b = lane < nw ? red[1][lane] : 0.0;
+        for (int k = 16; k > 0; k >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, k);
+            b += __shfl_xor_sync(0xffffffffu, b, k);
+        }
         if (lane == 0) {
-            atomicAdd(&sums[0], (double)a);
-            atomicAdd(&sums[1], (double)b);
+            sums[0] = a;
+            sums[1] = b;
         }
     }
 }
@@ -152,6 +184,10 @@ Window make_window() {
 
 size_t loss_scratch_floats(uint32_t width, uint32_t height) { return (size_t)width * height * (15 + 9 + 9); }
 
+size_t loss_sum_doubles(uint32_t width, uint32_t height) {
+    return 2 + 2 * (size_t)((width + 127u) / 128u) * height * 3;
+}
+
 void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_t height, float lambda,
                          float* scratch, double* sums, float* dl, cudaStream_t s) {
     const Window win = make_window();
@@ -159,11 +195,11 @@ void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_
     float* hm = scratch;
     float* partial = hm + 15 * P;
     float* hp = partial + 9 * P;
-    cudaMemsetAsync(sums, 0, 2 * sizeof(double), s);
     const dim3 block(128);
     const uint32_t bx = (width + 127u) / 128u;
     k_moments_h<<<dim3(bx, height, 3), block, 0, s>>>(x, y, width, height, win, hm);
-    k_moments_v<<<dim3(bx, height, 3), block, 0, s>>>(hm, x, y, width, height, win, partial, sums);
+    k_moments_v<<<dim3(bx, height, 3), block, 0, s>>>(hm, x, y, width, height, win, partial, sums + 2);
+    k_reduce_sums<<<1, 1024, 0, s>>>(sums, (size_t)bx * height * 3);
     if (dl) {
         k_partial_h<<<dim3(bx, height, 9), block, 0, s>>>(partial, width, height, win, hp);
         k_partial_v<<<dim3(bx, height, 3), block, 0, s>>>(hp, x, y, width, height, win, lambda, dl);

@@ -244,37 +244,54 @@ __global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ ro
     meta[g] = make_uint4((minTileY << 16u) | minTileX, (maxTileY << 16u) | maxTileX, depthU16, 0u);
 }
 
-// packed[block][g*width + c] -> rows[row][g]; one thread per (row, Gaussian).
-__global__ void k_pack_to_rows(const float* __restrict__ packed, uint32_t n, uint32_t stride, float* __restrict__ rows) {
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t r = blockIdx.y;
-    if (g >= stride) return;
-    float v = 0.0f;
-    if (g < n) {
-        uint64_t base, width, c;
-        if (r < 3) { base = 0; width = 3; c = r; }
-        else if (r < 6) { base = 3ull * n; width = 3; c = r - 3; }
-        else if (r < 10) { base = 6ull * n; width = 4; c = r - 6; }
-        else if (r < 13) { base = 10ull * n; width = 3; c = r - 10; }
-        else if (r < 14) { base = 13ull * n; width = 1; c = 0; }
-        else { base = 14ull * n; width = 45; c = r - 14; }
-        v = packed[base + (uint64_t)g * width + c];
+// Attribute blocks of the packed layout (preprocess.wgsl:16-24): first row, floats per Gaussian, and
+// the block's offset in units of n floats.
+__device__ __forceinline__ void attr_block(uint32_t b, uint32_t& row0, uint32_t& width, uint32_t& off) {
+    switch (b) {
+        case 0: row0 = 0; width = 3; off = 0; break;     // positions
+        case 1: row0 = 3; width = 3; off = 3; break;     // log-scales
+        case 2: row0 = 6; width = 4; off = 6; break;     // rotations
+        case 3: row0 = 10; width = 3; off = 10; break;   // f_dc
+        case 4: row0 = 13; width = 1; off = 13; break;   // opacity
+        default: row0 = 14; width = 45; off = 14; break; // f_rest
     }
-    rows[(size_t)r * stride + g] = v;
+}
+constexpr uint32_t kTransposeGroup = 128;  // Gaussians per CTA of the layout transposes
+
+// packed -> rows. A CTA moves kTransposeGroup Gaussians of one attribute block: one coalesced read
+// of the block's contiguous chunk into shared memory, then one coalesced write per row. Padding
+// columns (n <= g < stride) are zeroed.
+__global__ void __launch_bounds__(256) k_pack_to_rows(const float* __restrict__ packed, uint32_t n, uint32_t stride,
+                                                      float* __restrict__ rows) {
+    __shared__ float s[kTransposeGroup * 45];
+    uint32_t row0, width, off;
+    attr_block(blockIdx.y, row0, width, off);
+    const uint32_t g0 = blockIdx.x * kTransposeGroup;
+    const uint32_t cnt = g0 < n ? min(kTransposeGroup, n - g0) : 0u;
+    const float* src = packed + (uint64_t)off * n + (uint64_t)g0 * width;
+    for (uint32_t i = threadIdx.x; i < cnt * width; i += blockDim.x) s[i] = src[i];
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < width * kTransposeGroup; i += blockDim.x) {
+        const uint32_t c = i / kTransposeGroup, lg = i % kTransposeGroup, g = g0 + lg;
+        if (g < stride) rows[(size_t)(row0 + c) * stride + g] = lg < cnt ? s[lg * width + c] : 0.0f;
+    }
 }
 
-__global__ void k_rows_to_pack(const float* __restrict__ rows, uint32_t n, uint32_t stride, float* __restrict__ packed) {
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t r = blockIdx.y;
-    if (g >= n) return;
-    uint64_t base, width, c;
-    if (r < 3) { base = 0; width = 3; c = r; }
-    else if (r < 6) { base = 3ull * n; width = 3; c = r - 3; }
-    else if (r < 10) { base = 6ull * n; width = 4; c = r - 6; }
-    else if (r < 13) { base = 10ull * n; width = 3; c = r - 10; }
-    else if (r < 14) { base = 13ull * n; width = 1; c = 0; }
-    else { base = 14ull * n; width = 45; c = r - 14; }
-    packed[base + (uint64_t)g * width + c] = rows[(size_t)r * stride + g];
+// rows -> packed, the same tiling in the other direction.
+__global__ void __launch_bounds__(256) k_rows_to_pack(const float* __restrict__ rows, uint32_t n, uint32_t stride,
+                                                      float* __restrict__ packed) {
+    __shared__ float s[kTransposeGroup * 45];
+    uint32_t row0, width, off;
+    attr_block(blockIdx.y, row0, width, off);
+    const uint32_t g0 = blockIdx.x * kTransposeGroup;
+    const uint32_t cnt = min(kTransposeGroup, n - g0);
+    for (uint32_t i = threadIdx.x; i < width * kTransposeGroup; i += blockDim.x) {
+        const uint32_t c = i / kTransposeGroup, lg = i % kTransposeGroup;
+        if (lg < cnt) s[lg * width + c] = rows[(size_t)(row0 + c) * stride + g0 + lg];
+    }
+    __syncthreads();
+    float* dst = packed + (uint64_t)off * n + (uint64_t)g0 * width;
+    for (uint32_t i = threadIdx.x; i < cnt * width; i += blockDim.x) dst[i] = s[i];
 }
 
 __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32_t n) {
@@ -291,13 +308,13 @@ void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const Vie
 }
 
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
-    dim3 grid((stride + 255u) / 256u, kRows);
+    dim3 grid((stride + kTransposeGroup - 1u) / kTransposeGroup, 6);
     k_pack_to_rows<<<grid, 256, 0, s>>>(packed, n, stride, rows);
 }
 
 void launch_rows_to_pack(const float* rows, uint32_t n, uint32_t stride, float* packed, cudaStream_t s) {
     if (n == 0) return;
-    dim3 grid((n + 255u) / 256u, kRows);
+    dim3 grid((n + kTransposeGroup - 1u) / kTransposeGroup, 6);
     k_rows_to_pack<<<grid, 256, 0, s>>>(rows, n, stride, packed);
 }
 
