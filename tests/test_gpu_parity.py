@@ -125,3 +125,33 @@ def test_scene_scale_config_parity(gpu_ctx):
     packed = W.SCENE_1M.build()
     g, o = _run(gpu_ctx, packed, W.SCENE_1M.count, W.CAMERA_1080P.view())
     assert_frame_parity(g, o)
+
+
+def _golden():
+    import json
+    from pathlib import Path
+
+    return json.loads((Path(__file__).parent / "golden" / "oracle_fixtures.json").read_text())
+
+
+@pytest.mark.parametrize("case", _golden(), ids=[c["name"] for c in _golden()])
+def test_gpu_matches_committed_fixtures(case):
+    """The GPU frame reproduces the committed digests (no CPU oracle run needed on the GPU host)."""
+    import hashlib
+
+    def digest(a):
+        return hashlib.sha256(memoryview(np.ascontiguousarray(a)).cast("B")).hexdigest()
+
+    kind, count, seed, clusters, box = case["scene"]
+    packed = webgs.synth_scene(kind, count, seed, clusters, box)
+    assert digest(packed) == case["scene_digest"]
+    view = webgs.view_from_bytes(bytes.fromhex(case["view_hex"]))
+    with webgs.Context(tile_size=case["tile"], max_instance_factor=case["factor"]) as ctx:
+        scene = ctx.upload(packed, count)
+        out = ctx.forward(scene, view, rgba8=True, rgb=True, allow_overflow=True)
+        dbg = ctx.debug()
+        scene.close()
+    assert dbg["instance_count"] == case["instance_count"] and dbg["sorted_count"] == case["sorted_count"]
+    assert digest(dbg["keys"]) == case["keys"] and digest(dbg["vals"]) == case["vals"]
+    assert digest(dbg["ranges"]) == case["ranges"]
+    assert digest(out["rgb"]) == case["rgb"] and digest(out["rgba8"]) == case["rgba8"]
