@@ -196,6 +196,12 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t key_bits, int32_t location);
 /* Exclusive scan in place (offset_scan.wgsl:22-67); *total receives the sum (host pointer). */
 int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, int32_t location);
+/* Failure-path check (no counterpart in the reference): runs a scan whose lookback waits on a
+ * partition that never publishes. The wait gives up after its iteration limit (about a second), the
+ * kernel records the timeout in the device status word and returns; the call returns
+ * GS_ERR_TIMEOUT and the context stays usable. */
+int gs_check_wait_timeout(gs_ctx* ctx);
+
 /* The pinned fp32 exp of the kernels, evaluated on the device (y = exp(x)). */
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
 
@@ -224,6 +230,14 @@ int gs_camera_view(const float eye[3], const float target[3], const float up[3],
  * attributes: log-scale N(-4, 0.5^2), quaternion N(0,1)^4 normalised, opacity logit N(0, 1.5^2),
  * DC N(0, 0.5^2), rest N(0, 0.05^2). Bit-identical on every host. */
 int gs_synth_scene(uint32_t kind, uint32_t count, uint64_t seed, uint32_t clusters, float box, float* packed);
+
+/* Parses a binary little-endian .ply scene, as loadPly does (src/loader/loader.js:56-213): the header
+ * up to "end_header" (+ optional CR, LF), a vertex element whose scalar properties of any PLY type
+ * include x y z, scale_0..2, rot_0..3, opacity, f_dc_0..2 and f_rest_0..44 (others are skipped),
+ * vertex records starting right after the header. Writes *count and, when packed is not NULL,
+ * 59*count floats in the packed layout gs_scene_upload takes. Returns GS_ERR_INVALID with the
+ * reference's message in err (may be NULL) for a malformed file. */
+int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, float* packed, char* err, size_t err_len);
 
 /* Perturbs a packed scene in place: means += N(0, sigma_mean^2), SH (DC and rest) += N(0, sigma_sh^2). */
 int gs_perturb_scene(float* packed, uint32_t count, uint64_t seed, float sigma_mean, float sigma_sh);

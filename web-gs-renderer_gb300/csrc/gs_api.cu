@@ -1047,6 +1047,30 @@ int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, 
     return status_to_code(ctx, ctx->h_aux->status);
 }
 
+int gs_check_wait_timeout(gs_ctx* ctx) {
+    if (!ctx) return GS_ERR_INVALID;
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    // a two-partition scan run by one CTA that is handed the second partition's ticket: its lookback
+    // waits for the first partition's word, which nothing writes
+    const uint32_t n = 2 * kScanPartition;
+    GS_CK(ctx->aux_u32.reserve((size_t)n + 1));
+    const size_t words = (size_t)n / kScanPartition + 1;
+    if (words > ctx->aux_flags.cap || !ctx->aux_flags.p) {
+        GS_CK(ctx->aux_flags.reserve(words));
+        GS_CK(cudaMemsetAsync(ctx->aux_flags.p, 0, ctx->aux_flags.cap * 8, ctx->stream));
+    }
+    GS_CK(cudaMemsetAsync(ctx->aux_u32.p, 0, ((size_t)n + 1) * 4, ctx->stream));
+    FrameCtl* ctl = ctx->aux_ctl.p;
+    launch_frame_begin(ctl, ctx->stream);
+    static const uint32_t kOne = 1u;
+    GS_CK(cudaMemcpyAsync(&ctl->tickets[0], &kOne, sizeof(kOne), cudaMemcpyHostToDevice, ctx->stream));
+    launch_exclusive_scan(ctx->aux_u32.p, n, ctx->aux_u32.p + n, ctl, ctx->aux_flags.p, 0, ctx->stream, 1);
+    GS_CK(cudaGetLastError());
+    GS_CK(cudaMemcpyAsync(ctx->h_aux, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    return status_to_code(ctx, ctx->h_aux->status);
+}
+
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {
     if (!ctx) return GS_ERR_INVALID;
     if ((!x || !y) && n) return fail(ctx, GS_ERR_INVALID, "gs_exp_f32: null buffer");

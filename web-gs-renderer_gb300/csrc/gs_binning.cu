@@ -443,9 +443,9 @@ void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uin
 }
 
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
-                           uint32_t slot, cudaStream_t s) {
+                           uint32_t slot, cudaStream_t s, uint32_t grid) {
     const uint32_t parts = n == 0 ? 1u : (n + kScanPartition - 1u) / kScanPartition;
-    k_exclusive_scan<<<parts, kScanThreads, 0, s>>>(data, n, total_dev, ctl, flags, slot);
+    k_exclusive_scan<<<grid ? min(grid, parts) : parts, kScanThreads, 0, s>>>(data, n, total_dev, ctl, flags, slot);
 }
 
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,

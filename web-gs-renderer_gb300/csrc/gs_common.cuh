@@ -13,9 +13,10 @@ namespace gs {
 constexpr uint32_t kDevOverflow = 1u;
 constexpr uint32_t kDevTimeout = 2u;
 
-// Bounded spin: a wait on another CTA's publication gives up after this many polls, records
+// Bounded spin: a wait on another CTA's publication gives up after this many polls (about a
+// second with the back-off below; a healthy predecessor publishes within microseconds), records
 // kDevTimeout and returns, so no kernel can hang the GPU.
-constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kSpinLimit = 1u << 20;
 
 // Scene attribute rows of the device (structure-of-arrays) layout, one row of `stride` floats each.
 constexpr int kRowPos = 0;      // x, y, z

@@ -1,9 +1,13 @@
 // gs_host.cpp -- host utilities of libwebgs.so that need no GPU: the camera uniform builder and
 // the seeded synthetic scene generator. Compiled with -ffp-contract=off so that results are
 // bit-identical on x86-64 and aarch64 hosts.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "../../include/gs.h"
 
@@ -205,6 +209,151 @@ extern "C" int gs_synth_scene(uint32_t kind, uint32_t count, uint64_t seed, uint
         for (int a = 0; a < 45; ++a) rest[45 * g + a] = (float)(0.05 * normal01(seed, kRest, 45 * g + a));
     }
     delete[] ctab;
+    return GS_OK;
+}
+
+// ---- PLY ingest: src/loader/loader.js:56-213 restated -----------------------------------------------
+namespace {
+
+struct PlyProp {
+    std::string name;
+    int type;  // index into kPlyTypes
+    uint32_t offset;
+};
+struct PlyType {
+    const char* name;
+    uint32_t size;
+    int kind;  // 0 signed int, 1 unsigned int, 2 float32, 3 float64
+};
+const PlyType kPlyTypes[] = {
+    {"char", 1, 0},   {"uchar", 1, 1},  {"int8", 1, 0},    {"uint8", 1, 1},   {"short", 2, 0},   {"ushort", 2, 1},
+    {"int16", 2, 0},  {"uint16", 2, 1}, {"int", 4, 0},     {"uint", 4, 1},    {"int32", 4, 0},   {"uint32", 4, 1},
+    {"float", 4, 2},  {"float32", 4, 2}, {"double", 8, 3}, {"float64", 8, 3},
+};
+
+// loader.js:3-11: the 59 properties, in the order of the packed layout (loader.js:246-270)
+std::vector<std::string> required_properties() {
+    std::vector<std::string> r = {"x", "y", "z", "scale_0", "scale_1", "scale_2", "rot_0", "rot_1", "rot_2", "rot_3",
+                                  "f_dc_0", "f_dc_1", "f_dc_2", "opacity"};
+    for (int i = 0; i < 45; ++i) r.push_back("f_rest_" + std::to_string(i));
+    return r;
+}
+
+double read_le(const uint8_t* p, const PlyType& t) {  // DataView getters with littleEndian = true
+    uint64_t u = 0;
+    for (uint32_t i = 0; i < t.size; ++i) u |= (uint64_t)p[i] << (8 * i);
+    switch (t.kind) {
+        case 0: {
+            const uint32_t bits = 8 * t.size;
+            int64_t v = (int64_t)u;
+            if (bits < 64 && (u >> (bits - 1)) & 1u) v = (int64_t)(u | (~0ull << bits));
+            return (double)v;
+        }
+        case 1: return (double)u;
+        case 2: { uint32_t b = (uint32_t)u; float f; std::memcpy(&f, &b, 4); return (double)f; }
+        default: { double d; std::memcpy(&d, &u, 8); return d; }
+    }
+}
+
+int ply_fail(char* err, size_t err_len, const std::string& msg) {
+    if (err && err_len) {
+        const size_t k = std::min(err_len - 1, msg.size());
+        std::memcpy(err, msg.data(), k);
+        err[k] = '\0';
+    }
+    return GS_ERR_INVALID;
+}
+
+}  // namespace
+
+extern "C" int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, float* packed, char* err,
+                            size_t err_len) {
+    if (!bytes || !count) return ply_fail(err, err_len, "Invalid PLY: null buffer");
+    // findHeaderEnd (loader.js:277-295): "end_header", then an optional "\r" and an optional "\n"
+    static const char kEnd[] = "end_header";
+    const size_t kEndLen = sizeof(kEnd) - 1;
+    size_t idx = size;
+    for (size_t i = 0; i + kEndLen <= size; ++i)
+        if (std::memcmp(bytes + i, kEnd, kEndLen) == 0) { idx = i; break; }
+    if (idx == size) return ply_fail(err, err_len, "Invalid PLY: \"end_header\" not found");
+    size_t body = idx + kEndLen;
+    if (body < size && bytes[body] == '\r') ++body;
+    if (body < size && bytes[body] == '\n') ++body;
+    // parseHeader (loader.js:310-373)
+    std::string header(reinterpret_cast<const char*>(bytes), body);
+    long long vcount = 0;
+    bool little = false, has_format = false;
+    std::string element;
+    std::vector<PlyProp> props;
+    uint32_t stride = 0;
+    size_t pos = 0;
+    while (pos <= header.size()) {
+        size_t nl = header.find('\n', pos);
+        if (nl == std::string::npos) nl = header.size();
+        std::vector<std::string> words;
+        std::string w;
+        for (size_t i = pos; i < nl; ++i) {
+            const char ch = header[i];
+            if (ch == ' ' || ch == '\t' || ch == '\r' || ch == '\v' || ch == '\f') {
+                if (!w.empty()) words.push_back(w);
+                w.clear();
+            } else {
+                w.push_back(ch);
+            }
+        }
+        if (!w.empty()) words.push_back(w);
+        pos = nl + 1;
+        if (words.empty()) continue;
+        if (words[0] == "format") {
+            has_format = true;
+            little = words.size() > 1 && words[1] == "binary_little_endian";
+        }
+        if (words[0] == "element") {
+            element = words.size() > 1 ? words[1] : "";
+            if (element == "vertex") vcount = words.size() > 2 ? std::atoll(words[2].c_str()) : 0;
+        }
+        if (words[0] == "property" && element == "vertex") {
+            if (words.size() > 1 && words[1] == "list")
+                return ply_fail(err, err_len, "Invalid PLY: list properties are not supported");
+            const std::string type = words.size() > 1 ? words[1] : "";
+            int t = -1;
+            for (int k = 0; k < (int)(sizeof(kPlyTypes) / sizeof(kPlyTypes[0])); ++k)
+                if (type == kPlyTypes[k].name) t = k;
+            if (t < 0) return ply_fail(err, err_len, "Invalid PLY: unknown property type \"" + type + "\"");
+            props.push_back({words.size() > 2 ? words[2] : "", t, stride});
+            stride += kPlyTypes[t].size;
+        }
+    }
+    if (!has_format) return ply_fail(err, err_len, "Invalid PLY: missing \"format\" line");
+    if (!little) return ply_fail(err, err_len, "Invalid PLY: unsupported format");
+    if (vcount <= 0) return ply_fail(err, err_len, "Invalid PLY: vertex count missing or zero");
+    if (vcount > 0xFFFFFFFFll) return ply_fail(err, err_len, "Invalid PLY: vertex count exceeds 2^32-1");
+    const std::vector<std::string> req = required_properties();
+    std::vector<const PlyProp*> map(req.size(), nullptr);
+    for (size_t r = 0; r < req.size(); ++r) {
+        for (const PlyProp& p : props)
+            if (p.name == req[r]) map[r] = &p;  // last definition wins, as Map(properties) does
+        if (!map[r]) return ply_fail(err, err_len, "Invalid PLY: missing required property \"" + req[r] + "\"");
+    }
+    const uint64_t n = (uint64_t)vcount;
+    if (body + n * stride > size) return ply_fail(err, err_len, "Invalid PLY: vertex data truncated");
+    *count = (uint32_t)n;
+    if (!packed) return GS_OK;
+    // loader.js:246-270: positions, scales, rotations, f_dc, opacity, f_rest blocks
+    const uint64_t width[6] = {3, 3, 4, 3, 1, 45};
+    uint64_t base[6];
+    base[0] = 0;
+    for (int b = 1; b < 6; ++b) base[b] = base[b - 1] + width[b - 1] * n;
+#pragma omp parallel for schedule(static)
+    for (int64_t gi = 0; gi < (int64_t)n; ++gi) {
+        const uint8_t* rec = bytes + body + (uint64_t)gi * stride;
+        size_t r = 0;
+        for (int b = 0; b < 6; ++b)
+            for (uint64_t c = 0; c < width[b]; ++c, ++r) {
+                const PlyProp* p = map[r];
+                packed[base[b] + (uint64_t)gi * width[b] + c] = (float)read_le(rec + p->offset, kPlyTypes[p->type]);
+            }
+    }
     return GS_OK;
 }
 

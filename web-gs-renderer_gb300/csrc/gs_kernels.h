@@ -44,9 +44,10 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
 // Digit histograms of all passes over the low key_bits bits, for a standalone sort.
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);
-// Standalone exclusive scan (decoupled lookback); total written to *total_dev.
+// Standalone exclusive scan (decoupled lookback); total written to *total_dev. grid 0: one CTA per
+// partition (the normal case); a smaller grid leaves partitions unprocessed (failure-path checks).
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
-                           uint32_t slot, cudaStream_t s);
+                           uint32_t slot, cudaStream_t s, uint32_t grid = 0);
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,
                         cudaStream_t s);

@@ -82,6 +82,22 @@ def synth_scene(kind: int, count: int, seed: int, clusters: int = 0, box: float 
     return out
 
 
+def load_ply(source) -> dict:
+    """loadPly (src/loader/loader.js:56-149): a binary little-endian .ply (path or bytes) ->
+    {"count": n, "packed": float32 array of 59*n}, the argument Renderer.upload_gs_data takes."""
+    data = source if isinstance(source, (bytes, bytearray, memoryview)) else open(source, "rb").read()
+    data = bytes(data)
+    lib = library()
+    n = C.c_uint32()
+    err = C.create_string_buffer(256)
+    rc = lib.gs_ply_parse(data, len(data), C.byref(n), None, err, 256)
+    if rc != _abi.GS_OK:
+        raise GsError(rc, err.value.decode())
+    packed = np.empty(n.value * FLOATS_PER_GAUSSIAN, dtype=np.float32)
+    _check(lib.gs_ply_parse(data, len(data), C.byref(n), _ptr(packed), err, 256), None, "gs_ply_parse")
+    return {"count": n.value, "packed": packed}
+
+
 def perturb_scene(packed: np.ndarray, count: int, seed: int, sigma_mean: float, sigma_sh: float) -> np.ndarray:
     out = np.array(packed, dtype=np.float32, copy=True)
     _check(library().gs_perturb_scene(_ptr(out), count, seed, sigma_mean, sigma_sh), None, "gs_perturb_scene")

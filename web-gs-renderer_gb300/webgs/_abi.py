@@ -110,11 +110,13 @@ SIGNATURES = [
     ("gs_sort_pairs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
     ("gs_exclusive_scan", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]),
     ("gs_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
+    ("gs_check_wait_timeout", C.c_int, [C.c_void_p]),
     ("gs_exclusive_scan_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("gs_camera_view", C.c_int, [C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
                                  C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.POINTER(View)]),
     ("gs_synth_scene", C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]),
     ("gs_perturb_scene", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_float]),
+    ("gs_ply_parse", C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
 ]
 
 _LIB = None
