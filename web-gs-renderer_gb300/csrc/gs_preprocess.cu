@@ -1,10 +1,11 @@
 // gs_preprocess.cu -- per-Gaussian preprocess (src/shaders/preprocess.wgsl:58-284) and the scene
 // layout conversions.
 //
-// One thread per Gaussian over the structure-of-arrays scene rows: every attribute load of a warp
-// is one 128-byte coalesced line, so the kernel streams the 236 bytes of a visible Gaussian at HBM
-// rate. The arithmetic follows the WGSL source order with no contraction (the file is built with
-// -fmad=false) so that every output bit equals the reference restatement.
+// One thread per Gaussian over the structure-of-arrays scene rows. Each CTA stages its 128-Gaussian
+// slice of the 59 rows in shared memory with bulk copies (TMA, one mbarrier), so the whole 30 KB is
+// in flight before any arithmetic starts and the kernel streams the scene at HBM rate. The
+// arithmetic follows the WGSL source order with no contraction (the file is built with -fmad=false)
+// so that every output bit equals the reference restatement.
 #include "gs_kernels.h"
 
 namespace gs {
@@ -34,19 +35,66 @@ __device__ __forceinline__ M3 tr33(const M3& a) {
     return t;
 }
 
-__global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
-                                                    const ViewBlock* __restrict__ vb, uint32_t tile,
-                                                    float4* __restrict__ rec, uint4* __restrict__ meta,
-                                                    uint32_t* __restrict__ counts, FrameCtl* ctl) {
+// ---- bulk-copy (TMA) staging helpers ------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// global -> shared bulk copy completing on `bar`; addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+
+constexpr uint32_t kPreGroup = 128;  // Gaussians (threads) per preprocess CTA
+
+// The CTA's 128-Gaussian slice of all 59 attribute rows is staged in shared memory by bulk copies
+// (cp.async.bulk, 59 x 512 bytes on one mbarrier, issued by one thread), so every CTA has its whole
+// 30 KB in flight at once; threads then read their attributes from shared memory.
+__global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
+                                                          const ViewBlock* __restrict__ vb, uint32_t tile,
+                                                          float4* __restrict__ rec, uint4* __restrict__ meta,
+                                                          uint32_t* __restrict__ counts, FrameCtl* ctl) {
+    __shared__ __align__(128) float s_rows[kRows][kPreGroup];
+    __shared__ __align__(8) uint64_t s_bar;
     __shared__ ViewBlock sv;
-    if (threadIdx.x < 44) reinterpret_cast<uint32_t*>(&sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(vb)[threadIdx.x];
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kPreGroup;
+    if (lt == 0) mbar_init(&s_bar, 1);
+    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
     __syncthreads();
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lt == 0 && g0 < stride) {
+        // stride and g0 are multiples of 64: every row slice starts 256-byte aligned and spans a
+        // multiple of 256 bytes
+        const uint32_t cols = min(kPreGroup, stride - g0);
+        mbar_expect_tx(&s_bar, kRows * cols * 4u);
+        for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+    }
+    if (g0 < stride) {
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0)) {
+            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
+                if (lt == 0) atomicOr(&ctl->status, kDevTimeout);
+                break;
+            }
+        }
+    }
+    auto attr = [&](int row) { return s_rows[row][lt]; };
+    const uint32_t g = g0 + lt;
     if (g == 0) counts[n] = 0u;  // the N+1-th scan entry (cleared by renderer.js:826)
-    const uint32_t gg = g < n ? g : 0u;  // out-of-range threads compute on entry 0, write nothing
-    const float px = __ldg(rows + (size_t)(kRowPos + 0) * stride + gg);
-    const float py = __ldg(rows + (size_t)(kRowPos + 1) * stride + gg);
-    const float pz = __ldg(rows + (size_t)(kRowPos + 2) * stride + gg);
+    const float px = g < n ? attr(kRowPos + 0) : 0.0f;  // out-of-range threads compute on zeros, write nothing
+    const float py = g < n ? attr(kRowPos + 1) : 0.0f;
+    const float pz = g < n ? attr(kRowPos + 2) : 0.0f;
 
     // uniforms.view * vec4f(position, 1.0f)  (:79)
     float pv[4], clip[4];
@@ -82,13 +130,13 @@ __global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ ro
     const float pixy = ((ndcy + 1.0f) * H - 1.0f) * 0.5f;
 
     // 3D covariance (:95-100): R * S * transpose(S) * transpose(R)
-    const float sx = pinned_expf(__ldg(rows + (size_t)(kRowScale + 0) * stride + g));
-    const float sy = pinned_expf(__ldg(rows + (size_t)(kRowScale + 1) * stride + g));
-    const float sz = pinned_expf(__ldg(rows + (size_t)(kRowScale + 2) * stride + g));
-    const float q0 = __ldg(rows + (size_t)(kRowQuat + 0) * stride + g);
-    const float q1 = __ldg(rows + (size_t)(kRowQuat + 1) * stride + g);
-    const float q2 = __ldg(rows + (size_t)(kRowQuat + 2) * stride + g);
-    const float q3 = __ldg(rows + (size_t)(kRowQuat + 3) * stride + g);
+    const float sx = pinned_expf(attr(kRowScale + 0));
+    const float sy = pinned_expf(attr(kRowScale + 1));
+    const float sz = pinned_expf(attr(kRowScale + 2));
+    const float q0 = attr(kRowQuat + 0);
+    const float q1 = attr(kRowQuat + 1);
+    const float q2 = attr(kRowQuat + 2);
+    const float q3 = attr(kRowQuat + 3);
     const float qlen = sqrtf(((q1 * q1 + q2 * q2) + q3 * q3) + q0 * q0);
     const float qx = q1 / qlen, qy = q2 / qlen, qz = q3 / qlen, qw = q0 / qlen;
     const float x2 = qx + qx, y2 = qy + qy, z2 = qz + qz;
@@ -177,7 +225,7 @@ __global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ ro
     const float radius = ceilf(3.0f * sqrtf(lambda));
 
     // conic and sigmoid opacity (:106-112, :203-205)
-    const float op_logit = __ldg(rows + (size_t)kRowOpacity * stride + g);
+    const float op_logit = attr(kRowOpacity);
     const float opacity = 1.0f / (1.0f + pinned_expf(-op_logit));
     const float conx = cc / det, cony = -cb / det, conz = ca / det;
 
@@ -206,13 +254,13 @@ __global__ void __launch_bounds__(256) k_preprocess(const float* __restrict__ ro
     float col[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
-        const float* rest = rows + (size_t)(kRowRest + 15 * ch) * stride + g;
-        float r = kShC0 * __ldg(rows + (size_t)(kRowDc + ch) * stride + g);
-        r = r - w[1] * __ldg(rest + 0 * (size_t)stride);
-        r = r + w[2] * __ldg(rest + 1 * (size_t)stride);
-        r = r - w[3] * __ldg(rest + 2 * (size_t)stride);
+        const int rest = kRowRest + 15 * ch;
+        float r = kShC0 * attr(kRowDc + ch);
+        r = r - w[1] * attr(rest + 0);
+        r = r + w[2] * attr(rest + 1);
+        r = r - w[3] * attr(rest + 2);
 #pragma unroll
-        for (int k = 3; k < 15; ++k) r = r + w[k + 1] * __ldg(rest + k * (size_t)stride);
+        for (int k = 3; k < 15; ++k) r = r + w[k + 1] * attr(rest + k);
         r = r + 0.5f;
         col[ch] = fmaxf(r, 0.0f);
     }
@@ -303,8 +351,8 @@ __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32
 
 void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
                        float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s) {
-    const uint32_t blocks = (n + 255u) / 256u;
-    k_preprocess<<<blocks > 0 ? blocks : 1u, 256, 0, s>>>(rows, stride, n, view, tile, rec, meta, counts, ctl);
+    const uint32_t blocks = (n + kPreGroup - 1u) / kPreGroup;
+    k_preprocess<<<blocks > 0 ? blocks : 1u, kPreGroup, 0, s>>>(rows, stride, n, view, tile, rec, meta, counts, ctl);
 }
 
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
