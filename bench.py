@@ -400,7 +400,25 @@ def fwd_bwd(spec, cam, packed, steps, warmup, local_rank) -> dict:
                                 webgs.GS_MEM_DEVICE))
     sc.close()
     ctx.close()
+
+    # per-pass times of the same step from a profiling context (CUDA events between the passes)
+    pctx = webgs.Context(device=local_rank, flags=webgs.GS_FLAG_DIFFERENTIABLE | webgs.GS_FLAG_PROFILE)
+    psc = pctx.upload(packed, n)
+    pimg = _abi.Image(webgs.GS_MEM_DEVICE, None, rgb.data_ptr(), None, None)
+    acc: dict[str, float] = {}
+    prof_steps = max(3, min(steps, 20))
+    for it in range(prof_steps + 1):
+        pctx._ck(lib.gs_forward(pctx.handle, psc.handle, C.byref(view), C.byref(pimg)))
+        pctx._ck(lib.gs_loss_l1_ssim(pctx.handle, rgb.data_ptr(), target.data_ptr(), w, h, 0.2, None,
+                                     dl.data_ptr(), webgs.GS_MEM_DEVICE))
+        pctx._ck(lib.gs_backward(pctx.handle, psc.handle, dl.data_ptr(), grads.data_ptr(), webgs.GS_MEM_DEVICE))
+        if it:
+            for k, v in pctx.timings().items():
+                acc[k] = acc.get(k, 0.0) + v["ms"] / prof_steps
+    psc.close()
+    pctx.close()
     return {"ms_per_step": round(ms, 4), "Mpix/s": round(w * h / ms / 1e3, 2), "loss": round(loss.value, 6),
+            "passes_ms": {k: round(v, 4) for k, v in acc.items()},
             "workload": f"{n} Gaussians {w}x{h}, L1 + 0.2(1-SSIM) vs perturbed-scene target, grads of 59*N floats"}
 
 

@@ -106,6 +106,24 @@ def test_equal_depth_ties_keep_gaussian_order(gpu_ctx):
     assert same.any() and (v[1:][same] > v[:-1][same]).all()
 
 
+@pytest.mark.parametrize("seed", [21, 22])
+def test_needle_splats_parity(gpu_ctx, seed):
+    """Very anisotropic splats (one long axis, two thin ones, random orientation, high opacity): the
+    thin rotated ellipses stress the warp cull, whose skipped splats must be exactly those every pixel
+    of the warp rejects."""
+    n = 20_000
+    rng = np.random.default_rng(seed)
+    packed = W.SceneSpec(n, seed, 0).build()
+    scale = packed[3 * n: 6 * n].reshape(n, 3)
+    scale[:] = np.log(rng.uniform(0.0005, 0.004, (n, 3))).astype(np.float32)
+    scale[np.arange(n), rng.integers(0, 3, n)] = np.log(rng.uniform(0.02, 0.25, n)).astype(np.float32)
+    packed[13 * n: 14 * n] = rng.uniform(1.0, 6.0, n).astype(np.float32)  # opacity logits
+    view = W.CameraSpec((0.3, -0.2, -3.5), (0.0, 0.0, 0.0), 60.0, 480, 320).view()
+    g, o = _run(gpu_ctx, packed, n, view)
+    assert o["max_instance"] > o["instance_count"] > 200_000
+    assert_frame_parity(g, o)
+
+
 def test_repeat_frames_are_deterministic(gpu_ctx):
     packed = W.SceneSpec(30_000, 10, 0).build()
     view = W.CameraSpec((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 60.0, 320, 240).view()

@@ -783,7 +783,7 @@ static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const 
                            f.grad2d.p, s);
     if (ev) cudaEventRecord(ev[1], s);
     launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p,
-                               ctx->grows.p, accumulate, s);
+                               ctx->grows.p, accumulate, &f.ctl.p->status, s);
     if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
     return GS_OK;
@@ -823,10 +823,13 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
         dl = f.dl_stage.p;
     }
     const bool profile = (ctx->cfg.flags & GS_FLAG_PROFILE) != 0;
-    const int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream, profile ? ctx->bev : nullptr);
+    int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream, profile ? ctx->bev : nullptr);
     if (rc != GS_OK) return rc;
     ctx->have_bwd = profile;
-    return finish_grads(ctx, scene, grad_packed, location);
+    GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    rc = finish_grads(ctx, scene, grad_packed, location);
+    if (rc != GS_OK) return rc;
+    return location == GS_MEM_HOST ? status_to_code(ctx, f.h_ctl->status & kDevTimeout) : GS_OK;
 }
 
 int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
@@ -869,7 +872,15 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
         GS_CK(cudaEventRecord(ctx->join[s], ctx->side[s]));
         GS_CK(cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0));
     }
-    return finish_grads(ctx, scene, grad_packed, location);
+    for (uint32_t i = 0; i < count; ++i) {
+        Frame& f = *ctx->batch[i];
+        GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    const int rc = finish_grads(ctx, scene, grad_packed, location);
+    if (rc != GS_OK || location != GS_MEM_HOST) return rc;
+    uint32_t status = 0;
+    for (uint32_t i = 0; i < count; ++i) status |= ctx->batch[i]->h_ctl->status;
+    return status_to_code(ctx, status & kDevTimeout);  // an overflow was reported by the forward
 }
 
 int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t width, uint32_t height,

@@ -2,9 +2,10 @@
 // renders). Two kernels:
 //   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
 //                         contributor, recomputing power and alpha bit for bit as the forward did
-//                         (same warp cull, same pinned arithmetic), recovering T by division, and
-//                         accumulating dL/d(pixel.xy, conic, opacity, colour) per Gaussian: the 32
-//                         lanes of a warp reduce by shuffles, one lane issues the atomics;
+//                         (same pinned arithmetic, a conservative warp cull), recovering T by
+//                         division, and accumulating dL/d(pixel.xy, conic, opacity, colour) per
+//                         Gaussian: two pixels per lane, the warp reduces by shuffles, nine lanes
+//                         issue the atomics;
 //   k_preprocess_backward one thread per visible Gaussian: chain rule back through colour (SH),
 //                         sigmoid, conic inverse, 2D covariance J W Sigma W^T J^T, the rotation /
 //                         scale factorisation, and the projection, into the 59 attribute rows.
@@ -13,48 +14,10 @@
 // pass none; where the frustum guard clamps t.x/t.z (t.y/t.z) no gradient flows through t.x (t.y),
 // as in 3DGS.
 #include "gs_kernels.h"
+#include "gs_raster_common.cuh"
 
 namespace gs {
 namespace {
-
-__device__ __forceinline__ float raster_expf_b(float x) {  // identical to the forward raster's exp
-    const float n = rintf(__fmul_rn(x, 0x1.715476p+0f));
-    float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
-    r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
-    float p = 0x1.a01a02p-13f;
-    p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
-    p = __fmaf_rn(p, r, 0x1.111112p-7f);
-    p = __fmaf_rn(p, r, 0x1.555556p-5f);
-    p = __fmaf_rn(p, r, 0x1.555556p-3f);
-    p = __fmaf_rn(p, r, 0.5f);
-    p = __fmaf_rn(p, r, 1.0f);
-    p = __fmaf_rn(p, r, 1.0f);
-    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
-}
-
-__device__ __forceinline__ bool finite_b(float v) { return fabsf(v) <= 3.0e38f; }
-
-// Same cull box as the forward raster (see gs_raster.cu for the bound).
-__device__ __forceinline__ float4 cull_box_b(float x, float y, float a, float b, float c, float cut, float tx0,
-                                             float tx1, float ty0, float ty1) {
-    const float inf = __int_as_float(0x7f800000);
-    const float4 keep_all = make_float4(-inf, inf, -inf, inf);
-    if (!(finite_b(x) && finite_b(y) && finite_b(a) && finite_b(b) && finite_b(c)) || cut != cut) return keep_all;
-    if (!(a > 0.0f) || !(c > 0.0f)) return keep_all;
-    const float dxm = fmaxf(fabsf(x - tx0), fabsf(x - tx1));
-    const float dym = fmaxf(fabsf(y - ty0), fabsf(y - ty1));
-    const float smax = (a * dxm * dxm + c * dym * dym + 2.0f * fabsf(b) * dxm * dym) * 1.01f;
-    if (!finite_b(smax)) return keep_all;
-    if (cut > 0.0f) return make_float4(inf, -inf, inf, -inf);
-    const float ac = a * c, bb = b * b;
-    const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
-    if (!(det_lo > 0.0f)) return keep_all;
-    const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
-    const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
-    const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
-    if (!finite_b(hx) || !finite_b(hy)) return keep_all;
-    return make_float4(x - hx, x + hx, y - hy, y + hy);
-}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -90,61 +53,128 @@ __device__ __forceinline__ float warp_reduce_scatter8(const float v[8]) {
     return t;
 }
 
+// One pixel's backward state: its last contributor L (1-based position in the tile range), the
+// transmittance in front of the splat being visited, its colour gradient, and the colour blended
+// behind that splat (acc) with the previously visited splat's alpha and colour.
+struct PixState {
+    uint32_t L;
+    float fx, fy, T, dr, dg, db;
+    float acc_r, acc_g, acc_b, last_a, last_r, last_g, last_b;
+};
+
+__device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, uint32_t width, uint32_t height,
+                                         const float* __restrict__ final_t, const uint32_t* __restrict__ n_contrib,
+                                         const float* __restrict__ dl_drgb) {
+    p.fx = (float)x;
+    p.fy = (float)y;
+    p.L = 0;
+    p.T = 1.0f;
+    p.dr = p.dg = p.db = 0.0f;
+    p.acc_r = p.acc_g = p.acc_b = p.last_a = p.last_r = p.last_g = p.last_b = 0.0f;
+    if (x < width && y < height) {
+        const size_t q = (size_t)y * width + x;
+        p.L = n_contrib[q];
+        p.T = final_t[q];
+        p.dr = dl_drgb[3 * q];
+        p.dg = dl_drgb[3 * q + 1];
+        p.db = dl_drgb[3 * q + 2];
+    }
+}
+
+// Visits the splat at 1-based range position pos for one pixel: the same power / exp / alpha
+// decisions as the forward (bit for bit), then adds this pixel's share of the splat's gradients to
+// g = {d px, d py, d conic.x, d conic.y, d conic.z, d opacity, d r, d g, d b}. T is recovered by
+// division; the approximate divide (2 ulp, denominator >= 0.01) is accurate enough for a gradient.
+__device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4& a, const float4& b,
+                                         const float2& c, float g[9]) {
+    if (pos > p.L) return false;
+    const float dx = a.x - p.fx, dy = a.y - p.fy;
+    const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
+    if (power > 0.0f || power < c.y) return false;
+    const float G = raster_expf(power);
+    const float og = b.y * G;
+    const float alpha = fminf(kAlphaClamp, og);
+    if (!(alpha >= kEpsilon)) return false;
+    const float Tb = __fdividef(p.T, 1.0f - alpha);  // transmittance in front of this splat
+    p.acc_r = p.last_a * p.last_r + (1.0f - p.last_a) * p.acc_r;
+    p.acc_g = p.last_a * p.last_g + (1.0f - p.last_a) * p.acc_g;
+    p.acc_b = p.last_a * p.last_b + (1.0f - p.last_a) * p.acc_b;
+    const float w = alpha * Tb;
+    g[6] += w * p.dr;
+    g[7] += w * p.dg;
+    g[8] += w * p.db;
+    const float dalpha = Tb * ((b.z - p.acc_r) * p.dr + (b.w - p.acc_g) * p.dg + (c.x - p.acc_b) * p.db);
+    if (og <= kAlphaClamp) {
+        const float gp = dalpha * og;  // dL/dpower
+        g[0] += gp * (-a.z * dx - a.w * dy);
+        g[1] += gp * (-b.x * dy - a.w * dx);
+        g[2] += gp * -0.5f * dx * dx;
+        g[3] += gp * -dx * dy;
+        g[4] += gp * -0.5f * dy * dy;
+        g[5] += dalpha * G;
+    }
+    p.last_a = alpha;
+    p.last_r = b.z;
+    p.last_g = b.w;
+    p.last_b = c.x;
+    p.T = Tb;
+    return true;
+}
+
+// One CTA per tile with TILE*TILE/2 threads: each warp owns an 8x8 pixel block and each lane two
+// pixels of it, (x, y) and (x, y + 4), so the per-splat warp reduction and shared-memory loads are
+// shared by two pixels. A warp walks only positions up to the largest last-contributor index of its
+// own pixels.
 template <int TILE, int BATCH>
-__global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t* __restrict__ ranges,
-                                                                 const uint32_t* __restrict__ vals,
-                                                                 const float4* __restrict__ rec, uint32_t n,
-                                                                 const FrameCtl* __restrict__ ctl, uint32_t width,
-                                                                 uint32_t height, uint32_t tiles_x,
-                                                                 const float* __restrict__ final_t,
-                                                                 const uint32_t* __restrict__ n_contrib,
-                                                                 const float* __restrict__ dl_drgb,
-                                                                 float* __restrict__ grad2d) {
+__global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint32_t* __restrict__ ranges,
+                                                                     const uint32_t* __restrict__ vals,
+                                                                     const float4* __restrict__ rec, uint32_t n,
+                                                                     const FrameCtl* __restrict__ ctl,
+                                                                     uint32_t width, uint32_t height,
+                                                                     uint32_t tiles_x,
+                                                                     const float* __restrict__ final_t,
+                                                                     const uint32_t* __restrict__ n_contrib,
+                                                                     const float* __restrict__ dl_drgb,
+                                                                     float* __restrict__ grad2d) {
     constexpr int WX = TILE / 8;
+    constexpr int kThreads = TILE * TILE / 2;
     __shared__ float4 s_a[BATCH];
     __shared__ float4 s_b[BATCH];
     __shared__ float2 s_c[BATCH];
     __shared__ float4 s_box[BATCH];
+    __shared__ float4 s_ell[BATCH];
     __shared__ uint32_t s_g[BATCH];
     __shared__ uint32_t s_maxl;
 
     const uint32_t tile = blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 4u * (warp / WX);
+    const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 8u * (warp / WX);
     const uint32_t x = bx0 + (lane & 7u), y = by0 + (lane >> 3);
-    const bool inside = x < width && y < height;
     const uint2 range = reinterpret_cast<const uint2*>(ranges)[tile];
     const uint32_t end = ctl ? min(range.y, ctl->sorted_count) : range.y;
     const uint32_t start = range.x;
-    const float fx = (float)x, fy = (float)y;
-    const float rx0 = (float)bx0, rx1 = (float)(bx0 + 7u), ry0 = (float)by0, ry1 = (float)(by0 + 3u);
+    const uint32_t len = end > start ? end - start : 0u;
+    const float rx0 = (float)bx0, rx1 = (float)(bx0 + 7u), ry0 = (float)by0, ry1 = (float)(by0 + 7u);
     const float tx0 = (float)(tx * TILE), tx1 = (float)(tx * TILE + TILE - 1u);
     const float ty0 = (float)(ty * TILE), ty1 = (float)(ty * TILE + TILE - 1u);
 
-    uint32_t L = 0;
-    float T = 1.0f, dr = 0.0f, dg = 0.0f, db = 0.0f;
-    if (inside) {
-        const size_t p = (size_t)y * width + x;
-        L = n_contrib[p];
-        T = final_t[p];
-        dr = dl_drgb[3 * p];
-        dg = dl_drgb[3 * p + 1];
-        db = dl_drgb[3 * p + 2];
-    }
+    PixState p0, p1;
+    pix_load(p0, x, y, width, height, final_t, n_contrib, dl_drgb);
+    pix_load(p1, x, y + 4u, width, height, final_t, n_contrib, dl_drgb);
+    const uint32_t wmax = min(__reduce_max_sync(0xffffffffu, max(p0.L, p1.L)), len);
     if (threadIdx.x == 0) s_maxl = 0;
     __syncthreads();
-    if (L) atomicMax(&s_maxl, L);
+    if (lane == 0 && wmax) atomicMax(&s_maxl, wmax);
     __syncthreads();
-    const uint32_t maxl = min(s_maxl, end > start ? end - start : 0u);
-    float acc_r = 0.0f, acc_g = 0.0f, acc_b = 0.0f, last_a = 0.0f, last_r = 0.0f, last_g = 0.0f, last_b = 0.0f;
+    const uint32_t maxl = s_maxl;
 
     // positions are 1-based within the tile range; walk batches (lo, hi] from the top down
     for (uint32_t hi = maxl; hi > 0;) {
         const uint32_t lo = hi > (uint32_t)BATCH ? hi - BATCH : 0u;
         const uint32_t cnt = hi - lo;
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < cnt; j += TILE * TILE) {
+        for (uint32_t j = threadIdx.x; j < cnt; j += kThreads) {
             const uint32_t g = vals[start + lo + j];
             if (g < n) {
                 const float4 r0 = __ldg(rec + (size_t)kRecFloat4 * g);
@@ -153,7 +183,9 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t*
                 s_a[j] = r0;
                 s_b[j] = r1;
                 s_c[j] = make_float2(r2.x, r2.y);
-                s_box[j] = cull_box_b(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                const CullShape cs = cull_shape(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                s_box[j] = cs.box;
+                s_ell[j] = cs.ell;
                 s_g[j] = g;
             } else {
                 const float inf = __int_as_float(0x7f800000);
@@ -162,71 +194,35 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t*
             }
         }
         __syncthreads();
-        // groups of 32 from the top of the batch down, splats in a group from high to low
-        for (int gtop = (int)cnt - 1; gtop >= 0; gtop -= 32) {
-            const int gbase = gtop - 31;
-            const int jj = gbase + (int)lane;
-            bool hit = false;
-            if (jj >= 0) {
-                const float4 bx = s_box[jj];
-                hit = bx.y >= rx0 && bx.x <= rx1 && bx.w >= ry0 && bx.z <= ry1;
-            }
-            uint32_t m = __ballot_sync(0xffffffffu, hit);
-            while (m) {
-                const int bit = 31 - __clz(m);
-                m &= ~(1u << bit);
-                const int j = gbase + bit;
-                const uint32_t pos = lo + (uint32_t)j + 1u;
-                float g_px = 0.0f, g_py = 0.0f, g_a = 0.0f, g_b = 0.0f, g_c = 0.0f, g_o = 0.0f;
-                float g_r = 0.0f, g_g = 0.0f, g_bl = 0.0f;
-                bool contrib = false;
-                if (pos <= L) {
+        if (lo < wmax) {
+            // groups of 32 from the warp's top position in this batch down, splats in a group from
+            // high to low
+            const int top = (int)min(cnt, wmax - lo) - 1;
+            for (int gtop = top; gtop >= 0; gtop -= 32) {
+                const int gbase = gtop - 31;
+                const int jj = gbase + (int)lane;
+                const bool hit = jj >= 0 && block_meets(s_box[jj], s_ell[jj], s_a[jj], rx0, rx1, ry0, ry1);
+                uint32_t m = __ballot_sync(0xffffffffu, hit);
+                while (m) {
+                    const int bit = 31 - __clz(m);
+                    m &= ~(1u << bit);
+                    const int j = gbase + bit;
+                    const uint32_t pos = lo + (uint32_t)j + 1u;
                     const float4 a = s_a[j];
                     const float4 b = s_b[j];
                     const float2 c = s_c[j];
-                    const float dx = a.x - fx, dy = a.y - fy;
-                    const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
-                    if (!(power > 0.0f) && !(power < c.y)) {
-                        const float G = raster_expf_b(power);
-                        const float og = b.y * G;
-                        const float alpha = fminf(kAlphaClamp, og);
-                        if (alpha >= kEpsilon) {
-                            contrib = true;
-                            const float Tb = T / (1.0f - alpha);  // transmittance in front of this splat
-                            acc_r = last_a * last_r + (1.0f - last_a) * acc_r;
-                            acc_g = last_a * last_g + (1.0f - last_a) * acc_g;
-                            acc_b = last_a * last_b + (1.0f - last_a) * acc_b;
-                            const float w = alpha * Tb;
-                            g_r = w * dr;
-                            g_g = w * dg;
-                            g_bl = w * db;
-                            const float dalpha = Tb * ((b.z - acc_r) * dr + (b.w - acc_g) * dg + (c.x - acc_b) * db);
-                            if (og <= kAlphaClamp) {
-                                const float gp = dalpha * og;  // dL/dpower
-                                g_px = gp * (-a.z * dx - a.w * dy);
-                                g_py = gp * (-b.x * dy - a.w * dx);
-                                g_a = gp * -0.5f * dx * dx;
-                                g_b = gp * -dx * dy;
-                                g_c = gp * -0.5f * dy * dy;
-                                g_o = dalpha * G;
-                            }
-                            last_a = alpha;
-                            last_r = b.z;
-                            last_g = b.w;
-                            last_b = c.x;
-                            T = Tb;
+                    float g[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                    const bool c0 = pix_step(p0, pos, a, b, c, g);
+                    const bool c1 = pix_step(p1, pos, a, b, c, g);
+                    if (__any_sync(0xffffffffu, c0 || c1)) {
+                        const float mine = warp_reduce_scatter8(g);  // total of value (lane >> 2) & 7
+                        const float blue = warp_sum(g[8]);
+                        const uint32_t gi = s_g[j];
+                        if (gi < n) {
+                            float* dst = grad2d + (size_t)9 * gi;
+                            if ((lane & 3u) == 0u) atomicAdd(dst + ((lane >> 2) & 7u), mine);
+                            if (lane == 2u) atomicAdd(dst + 8, blue);
                         }
-                    }
-                }
-                if (__any_sync(0xffffffffu, contrib)) {
-                    const float v8[8] = {g_px, g_py, g_a, g_b, g_c, g_o, g_r, g_g};
-                    const float mine = warp_reduce_scatter8(v8);  // total of value (lane >> 2) & 7
-                    const float blue = warp_sum(g_bl);
-                    const uint32_t gi = s_g[j];
-                    if (gi < n) {
-                        float* dst = grad2d + (size_t)9 * gi;
-                        if ((lane & 3u) == 0u) atomicAdd(dst + ((lane >> 2) & 7u), mine);
-                        if (lane == 2u) atomicAdd(dst + 8, blue);
                     }
                 }
             }
@@ -236,26 +232,61 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster_backward(const uint32_t*
 }
 
 // ---- preprocess backward ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
-                                                             uint32_t n, const ViewBlock* __restrict__ vb,
-                                                             const uint32_t* __restrict__ counts,
-                                                             const float* __restrict__ grad2d,
-                                                             float* __restrict__ grows, int accumulate) {
+constexpr uint32_t kBwdGroup = 128;  // Gaussians (threads) per preprocess-backward CTA
+
+// One thread per Gaussian. A CTA with at least one visible Gaussian stages its 128-Gaussian slice
+// of the 59 attribute rows in shared memory with bulk copies on one mbarrier (as the forward
+// preprocess does), so all of its loads are in flight at once; a CTA with none only writes zeros.
+__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
+                                                                   uint32_t n, const ViewBlock* __restrict__ vb,
+                                                                   const uint32_t* __restrict__ counts,
+                                                                   const float* __restrict__ grad2d,
+                                                                   float* __restrict__ grows, int accumulate,
+                                                                   uint32_t* status) {
+    __shared__ __align__(128) float s_rows[kRows][kBwdGroup];
+    __shared__ __align__(8) uint64_t s_bar;
     __shared__ ViewBlock sv;
-    if (threadIdx.x < 44) reinterpret_cast<uint32_t*>(&sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(vb)[threadIdx.x];
-    __syncthreads();
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    auto R_ = [&](int row) { return __ldg(rows + (size_t)row * stride + g); };
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kBwdGroup;
+    const uint32_t g = g0 + lt;
+    const bool vis = g < n && counts[g] != 0u;
+    if (lt == 0) mbar_init(&s_bar, 1);
+    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
+    const int any = __syncthreads_or(vis);
     // accumulate: several views of one scene add into the same rows (FP32 atomics)
     auto W_ = [&](int row, float v) {
         float* dst = grows + (size_t)row * stride + g;
         if (accumulate) atomicAdd(dst, v); else *dst = v;
     };
-    if (counts[g] == 0u) {
-        for (int r = 0; r < kRows; ++r) W_(r, 0.0f);
+    auto zero_rows = [&]() {
+        if (!accumulate && g < n)
+            for (int r = 0; r < kRows; ++r) grows[(size_t)r * stride + g] = 0.0f;
+    };
+    if (!any) {
+        zero_rows();
         return;
     }
+    if (lt == 0) {
+        // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and spans
+        // a multiple of 256 bytes (g0 < n <= stride)
+        const uint32_t cols = min(kBwdGroup, stride - g0);
+        mbar_expect_tx(&s_bar, kRows * cols * 4u);
+        for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+    }
+    {
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0)) {
+            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
+                if (lt == 0 && status) atomicOr(status, kDevTimeout);
+                break;
+            }
+        }
+    }
+    if (!vis) {
+        zero_rows();
+        return;
+    }
+    auto R_ = [&](int row) { return s_rows[row][lt]; };
     const float* d2 = grad2d + (size_t)9 * g;
     const float gpx = d2[0], gpy = d2[1], gA = d2[2], gB = d2[3], gC = d2[4], go = d2[5];
     const float p[3] = {R_(0), R_(1), R_(2)};
@@ -356,15 +387,19 @@ __global__ void __launch_bounds__(256) k_preprocess_backward(const float* __rest
     Y[14] = kShC3_5 * dz_ * (xx - yy);
     Y[15] = kShC3_6 * dx_ * (xx - 3 * yy);
     float gcol[3];
+#pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
         float raw = Y[0] * R_(kRowDc + ch);
+#pragma unroll
         for (int k = 1; k < 16; ++k) raw += Y[k] * R_(kRowRest + (k - 1) + 15 * ch);
         raw += 0.5f;
         gcol[ch] = raw < 0.0f ? 0.0f : d2[6 + ch];
     }
     float wsh[16];
+#pragma unroll
     for (int k = 0; k < 16; ++k) {
         float acc = 0.0f;
+#pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
             const int row = k == 0 ? kRowDc + ch : kRowRest + (k - 1) + 15 * ch;
             acc += R_(row) * gcol[ch];
@@ -431,7 +466,7 @@ void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* val
                      const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
                      const float* final_t, const uint32_t* n_contrib, const float* dl, float* grad2d, cudaStream_t s) {
     const uint32_t grid = tiles_x * tiles_y;
-    constexpr int threads = TILE * TILE;
+    constexpr int threads = TILE * TILE / 2;
     switch (batch) {
         case 32: k_raster_backward<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
         case 64: k_raster_backward<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
@@ -456,10 +491,11 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
 
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
                                 const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
-                                cudaStream_t s) {
+                                uint32_t* status, cudaStream_t s) {
     if (n == 0) return;
-    k_preprocess_backward<<<(n + 255u) / 256u, 256, 0, s>>>(rows, stride, n, view, counts, grad2d, grows,
-                                                            accumulate ? 1 : 0);
+    k_preprocess_backward<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, 0, s>>>(rows, stride, n, view, counts,
+                                                                                grad2d, grows, accumulate ? 1 : 0,
+                                                                                status);
 }
 
 }  // namespace gs

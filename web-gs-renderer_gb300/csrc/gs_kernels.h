@@ -76,7 +76,7 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
 // accumulate: add into grows with FP32 atomics (several views of one scene) instead of storing.
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
                                 const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
-                                cudaStream_t s);
+                                uint32_t* status, cudaStream_t s);
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------
 size_t loss_scratch_floats(uint32_t width, uint32_t height);

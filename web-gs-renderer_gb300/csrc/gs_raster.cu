@@ -14,65 +14,18 @@
 //  * cut-off: a pixel whose power is below the splat's cut-off c_o = ln((1/255)/o) - 1e-3 skips
 //    the exp, since o*exp(power) < 1/255 is certain there (the 1e-3 margin is far beyond the
 //    rounding of exp, the product and logf);
-//  * warp cull: when staging a splat, the CTA bounds the region {power >= c_o} by the bounding box
-//    of the ellipse Q(d) <= K', Q = a dx^2 + 2b dx dy + c dy^2, K' = -2 c_o plus the worst rounding
-//    error of the pinned power formula anywhere in the tile (16 eps times the sum of the absolute
-//    terms, bounded over the tile), with det = ac - b^2 taken at its lower rounding bound. Every
-//    warp tests its 8x4 pixel block against the 32 boxes of a group in parallel (one box per lane,
-//    one ballot) and walks only the splats whose box meets its block, in range order. A skipped
-//    splat would have been rejected by every pixel of the warp at "power < c_o" (or "power > 0").
-//    Splats whose box cannot be bounded safely (non-positive-definite or non-finite values) are
-//    never culled. Contributor counts are range positions, so skipping does not change them.
+//  * warp cull: when staging a splat, the CTA computes its cull shape for the tile (a bounding box of
+//    the region where power >= c_o can hold, and the data of an exact ellipse-versus-rectangle
+//    test; gs_raster_common.cuh gives the bounds). Every warp tests its 8x4 pixel block against the
+//    32 splats of a group in parallel (one splat per lane, one ballot) and walks only the splats
+//    that meet its block, in range order. A skipped splat would have been rejected by every pixel
+//    of the warp at "power < c_o" (or "power > 0"). Contributor counts are range positions, so
+//    skipping does not change them.
 #include "gs_kernels.h"
+#include "gs_raster_common.cuh"
 
 namespace gs {
 namespace {
-
-// The pinned exp restricted to the arguments the raster can reach. For an opacity o in (0, 1] the
-// cut-off is at least ln(1/255) - 1e-3 > -5.6, so every argument lies in [-5.6, 0]: no range
-// checks are needed and 2^n (n >= -9) is applied as one exact power-of-two factor, which gives the
-// same bits as pinned_expf's two-factor scaling. o = 0 (cut-off +inf) never gets here; for a NaN
-// opacity the product o * exp(.) is NaN whatever this returns, as with pinned_expf.
-__device__ __forceinline__ float raster_expf(float x) {
-    const float n = rintf(__fmul_rn(x, 0x1.715476p+0f));
-    float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
-    r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
-    float p = 0x1.a01a02p-13f;
-    p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
-    p = __fmaf_rn(p, r, 0x1.111112p-7f);
-    p = __fmaf_rn(p, r, 0x1.555556p-5f);
-    p = __fmaf_rn(p, r, 0x1.555556p-3f);
-    p = __fmaf_rn(p, r, 0.5f);
-    p = __fmaf_rn(p, r, 1.0f);
-    p = __fmaf_rn(p, r, 1.0f);
-    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
-}
-
-__device__ __forceinline__ bool finite(float v) { return fabsf(v) <= 3.0e38f; }
-
-// Conservative box (x0, x1, y0, y1) outside of which no pixel of the tile [tx0,tx1]x[ty0,ty1] can
-// reach power >= cut with the pinned arithmetic; (+inf, -inf, +inf, -inf) when no pixel can;
-// (-inf, +inf, -inf, +inf) when no safe bound exists.
-__device__ __forceinline__ float4 cull_box(float x, float y, float a, float b, float c, float cut, float tx0,
-                                           float tx1, float ty0, float ty1) {
-    const float inf = __int_as_float(0x7f800000);
-    const float4 keep_all = make_float4(-inf, inf, -inf, inf);
-    if (!(finite(x) && finite(y) && finite(a) && finite(b) && finite(c)) || cut != cut) return keep_all;
-    if (!(a > 0.0f) || !(c > 0.0f)) return keep_all;
-    const float dxm = fmaxf(fabsf(x - tx0), fabsf(x - tx1));
-    const float dym = fmaxf(fabsf(y - ty0), fabsf(y - ty1));
-    const float smax = (a * dxm * dxm + c * dym * dym + 2.0f * fabsf(b) * dxm * dym) * 1.01f;
-    if (!finite(smax)) return keep_all;
-    if (cut > 0.0f) return make_float4(inf, -inf, inf, -inf);  // power <= 0 < cut everywhere
-    const float ac = a * c, bb = b * b;
-    const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
-    if (!(det_lo > 0.0f)) return keep_all;
-    const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
-    const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
-    const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
-    if (!finite(hx) || !finite(hy)) return keep_all;
-    return make_float4(x - hx, x + hx, y - hy, y + hy);
-}
 
 template <int TILE, int BATCH>
 __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restrict__ ranges,
@@ -86,6 +39,7 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
     __shared__ float4 s_b[BATCH];    // (conic.z, opacity, r, g)
     __shared__ float2 s_c[BATCH];    // (b, cut)
     __shared__ float4 s_box[BATCH];  // cull box (x0, x1, y0, y1)
+    __shared__ float4 s_ell[BATCH];  // ellipse test data
 
     const uint32_t tile = blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
@@ -118,7 +72,9 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
                     s_a[j] = r0;
                     s_b[j] = r1;
                     s_c[j] = make_float2(r2.x, r2.y);
-                    s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                    const CullShape cs = cull_shape(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                    s_box[j] = cs.box;
+                    s_ell[j] = cs.ell;
                 } else {  // only after a timed-out sort: a splat that never blends
                     const float inf = __int_as_float(0x7f800000);
                     s_a[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -134,10 +90,8 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
         for (uint32_t g0 = 0; g0 < cnt; g0 += 32u) {
             if (__all_sync(0xffffffffu, done)) break;
             bool hit = false;
-            if (g0 + lane < cnt) {
-                const float4 bx = s_box[g0 + lane];
-                hit = bx.y >= rx0 && bx.x <= rx1 && bx.w >= ry0 && bx.z <= ry1;
-            }
+            if (g0 + lane < cnt)
+                hit = block_meets(s_box[g0 + lane], s_ell[g0 + lane], s_a[g0 + lane], rx0, rx1, ry0, ry1);
             uint32_t m = __ballot_sync(0xffffffffu, hit);
             while (m) {
                 const uint32_t j = g0 + (uint32_t)(__ffs(m) - 1);
