@@ -396,6 +396,7 @@ int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
         return GS_ERR_CUDA;
     }
     if (cudaSetDevice(c.device) != cudaSuccess) return GS_ERR_CUDA;
+    configure_sort_kernels();
     gs_ctx* ctx = new gs_ctx();
     ctx->cfg = c;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -772,8 +773,9 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 }
 
 // ---- backward --------------------------------------------------------------------------------------
-// Raster backward of frame f into f.grad2d, then the preprocess backward into ctx->grows.
-static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, bool accumulate,
+// Raster backward of frame f into f.grad2d, then the preprocess backward: packed, into `out` in the
+// packed layout; else added into the rows of ctx->grows.
+static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, float* out, bool packed,
                             cudaStream_t s, cudaEvent_t* ev = nullptr) {
     GS_CK(f.grad2d.reserve((size_t)scene->n * 9));
     if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
@@ -782,8 +784,8 @@ static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const 
                            scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
                            f.grad2d.p, s);
     if (ev) cudaEventRecord(ev[1], s);
-    launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p,
-                               ctx->grows.p, accumulate, &f.ctl.p->status, s);
+    launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p, out,
+                               packed, &f.ctl.p->status, s);
     if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
     return GS_OK;
@@ -814,22 +816,26 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
     if (!f.valid || f.scene != scene || f.n != scene->n)
         return fail(ctx, GS_ERR_STATE, "gs_backward: the last gs_forward on this context was not on this scene");
     GS_CK(cudaSetDevice(ctx->cfg.device));
-    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
+    const size_t nfloats = (size_t)scene->n * kRows;
     const float* dl = dl_drgb;
+    float* out = grad_packed;
     if (location == GS_MEM_HOST) {
         const size_t pix = (size_t)f.width * f.height;
         GS_CK(f.dl_stage.reserve(pix * 3));
         GS_CK(cudaMemcpyAsync(f.dl_stage.p, dl_drgb, pix * 12, cudaMemcpyHostToDevice, ctx->stream));
         dl = f.dl_stage.p;
+        GS_CK(ctx->grad_stage.reserve(nfloats));
+        out = ctx->grad_stage.p;
     }
     const bool profile = (ctx->cfg.flags & GS_FLAG_PROFILE) != 0;
-    int rc = enqueue_backward(ctx, f, scene, dl, false, ctx->stream, profile ? ctx->bev : nullptr);
+    const int rc = enqueue_backward(ctx, f, scene, dl, out, true, ctx->stream, profile ? ctx->bev : nullptr);
     if (rc != GS_OK) return rc;
     ctx->have_bwd = profile;
     GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    rc = finish_grads(ctx, scene, grad_packed, location);
-    if (rc != GS_OK) return rc;
-    return location == GS_MEM_HOST ? status_to_code(ctx, f.h_ctl->status & kDevTimeout) : GS_OK;
+    if (location == GS_MEM_DEVICE) return GS_OK;
+    if (nfloats) GS_CK(cudaMemcpyAsync(grad_packed, out, nfloats * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    return status_to_code(ctx, f.h_ctl->status & kDevTimeout);
 }
 
 int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
@@ -865,7 +871,7 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
     const int used = (int)std::min<uint32_t>(count, kSideStreams);
     for (int s = 0; s < used; ++s) GS_CK(cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0));
     for (uint32_t i = 0; i < count; ++i) {
-        const int rc = enqueue_backward(ctx, *ctx->batch[i], scene, dls[i], true, ctx->side[i % used]);
+        const int rc = enqueue_backward(ctx, *ctx->batch[i], scene, dls[i], ctx->grows.p, false, ctx->side[i % used]);
         if (rc != GS_OK) return rc;
     }
     for (int s = 0; s < used; ++s) {

@@ -2,13 +2,14 @@
 // renders). Two kernels:
 //   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
 //                         contributor, recomputing power and alpha bit for bit as the forward did
-//                         (same pinned arithmetic, a conservative warp cull), recovering T by
+//                         (same pinned arithmetic, the forward's warp cull box), recovering T by
 //                         division, and accumulating dL/d(pixel.xy, conic, opacity, colour) per
 //                         Gaussian: two pixels per lane, the warp reduces by shuffles, nine lanes
 //                         issue the atomics;
-//   k_preprocess_backward one thread per visible Gaussian: chain rule back through colour (SH),
-//                         sigmoid, conic inverse, 2D covariance J W Sigma W^T J^T, the rotation /
-//                         scale factorisation, and the projection, into the 59 attribute rows.
+//   k_preprocess_backward one thread per Gaussian: chain rule back through colour (SH), sigmoid,
+//                         conic inverse, 2D covariance J W Sigma W^T J^T, the rotation / scale
+//                         factorisation, and the projection, into the 59 attributes (stored in
+//                         the packed input layout, or added into attribute rows for a batch).
 // Conventions: gradients flow through the fp32 RGB before quantization; culled Gaussians, skipped
 // pairs and splats after a pixel's termination get none; active clamps (alpha 0.99, colour >= 0)
 // pass none; where the frustum guard clamps t.x/t.z (t.y/t.z) no gradient flows through t.x (t.y),
@@ -142,7 +143,6 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
     __shared__ float4 s_b[BATCH];
     __shared__ float2 s_c[BATCH];
     __shared__ float4 s_box[BATCH];
-    __shared__ float4 s_ell[BATCH];
     __shared__ uint32_t s_g[BATCH];
     __shared__ uint32_t s_maxl;
 
@@ -183,9 +183,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                 s_a[j] = r0;
                 s_b[j] = r1;
                 s_c[j] = make_float2(r2.x, r2.y);
-                const CullShape cs = cull_shape(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
-                s_box[j] = cs.box;
-                s_ell[j] = cs.ell;
+                s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
                 s_g[j] = g;
             } else {
                 const float inf = __int_as_float(0x7f800000);
@@ -201,7 +199,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
             for (int gtop = top; gtop >= 0; gtop -= 32) {
                 const int gbase = gtop - 31;
                 const int jj = gbase + (int)lane;
-                const bool hit = jj >= 0 && block_meets(s_box[jj], s_ell[jj], s_a[jj], rx0, rx1, ry0, ry1);
+                const bool hit = jj >= 0 && box_meets(s_box[jj], rx0, rx1, ry0, ry1);
                 uint32_t m = __ballot_sync(0xffffffffu, hit);
                 while (m) {
                     const int bit = 31 - __clz(m);
@@ -233,61 +231,15 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
 
 // ---- preprocess backward ---------------------------------------------------------------------------
 constexpr uint32_t kBwdGroup = 128;  // Gaussians (threads) per preprocess-backward CTA
+// Floats per staged attribute row: rows start 16-byte aligned (bulk-copy destinations) and the
+// packed write-out reads them with at most 4-way bank conflicts.
+constexpr uint32_t kBwdPitch = 132;
 
-// One thread per Gaussian. A CTA with at least one visible Gaussian stages its 128-Gaussian slice
-// of the 59 attribute rows in shared memory with bulk copies on one mbarrier (as the forward
-// preprocess does), so all of its loads are in flight at once; a CTA with none only writes zeros.
-__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
-                                                                   uint32_t n, const ViewBlock* __restrict__ vb,
-                                                                   const uint32_t* __restrict__ counts,
-                                                                   const float* __restrict__ grad2d,
-                                                                   float* __restrict__ grows, int accumulate,
-                                                                   uint32_t* status) {
-    __shared__ __align__(128) float s_rows[kRows][kBwdGroup];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ ViewBlock sv;
-    const uint32_t lt = threadIdx.x;
-    const uint32_t g0 = blockIdx.x * kBwdGroup;
-    const uint32_t g = g0 + lt;
-    const bool vis = g < n && counts[g] != 0u;
-    if (lt == 0) mbar_init(&s_bar, 1);
-    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
-    const int any = __syncthreads_or(vis);
-    // accumulate: several views of one scene add into the same rows (FP32 atomics)
-    auto W_ = [&](int row, float v) {
-        float* dst = grows + (size_t)row * stride + g;
-        if (accumulate) atomicAdd(dst, v); else *dst = v;
-    };
-    auto zero_rows = [&]() {
-        if (!accumulate && g < n)
-            for (int r = 0; r < kRows; ++r) grows[(size_t)r * stride + g] = 0.0f;
-    };
-    if (!any) {
-        zero_rows();
-        return;
-    }
-    if (lt == 0) {
-        // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and spans
-        // a multiple of 256 bytes (g0 < n <= stride)
-        const uint32_t cols = min(kBwdGroup, stride - g0);
-        mbar_expect_tx(&s_bar, kRows * cols * 4u);
-        for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
-    }
-    {
-        uint32_t spins = 0;
-        while (!mbar_try_wait(&s_bar, 0)) {
-            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
-                if (lt == 0 && status) atomicOr(status, kDevTimeout);
-                break;
-            }
-        }
-    }
-    if (!vis) {
-        zero_rows();
-        return;
-    }
-    auto R_ = [&](int row) { return s_rows[row][lt]; };
-    const float* d2 = grad2d + (size_t)9 * g;
+// Chain rule of one visible Gaussian from its 2D gradients d2 = dL/d(pixel.xy, conic, opacity, rgb)
+// back to its 59 attributes. R_(row) reads an attribute, W_(row, v) emits its gradient; every W_ of a
+// row comes after the last R_ of that row, so W_ may overwrite the staged attribute in place.
+template <class RF, class WF>
+__device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const float* __restrict__ d2, RF R_, WF W_) {
     const float gpx = d2[0], gpy = d2[1], gA = d2[2], gB = d2[3], gC = d2[4], go = d2[5];
     const float p[3] = {R_(0), R_(1), R_(2)};
     float pv[4], clip[4];
@@ -461,6 +413,73 @@ __global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward(const float* 
     W_(kRowQuat + 3, (gq[2] - q[2] * qd) / qlen);
 }
 
+// One thread per Gaussian. A CTA with at least one visible Gaussian stages its 128-Gaussian slice of
+// the 59 attribute rows in shared memory with bulk copies on one mbarrier (as the forward preprocess
+// does), so all of its loads are in flight at once.
+//   PACKED  the gradients replace the staged attributes in shared memory and the CTA writes its
+//           slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest blocks, the
+//           layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros;
+//   !PACKED the gradients are added with FP32 atomics into 59 rows of `stride` floats (several views
+//           of one scene accumulate there; invisible Gaussians add nothing).
+template <bool PACKED>
+__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
+                                                                   uint32_t n, const ViewBlock* __restrict__ vb,
+                                                                   const uint32_t* __restrict__ counts,
+                                                                   const float* __restrict__ grad2d,
+                                                                   float* __restrict__ out, uint32_t* status) {
+    __shared__ __align__(128) float s_rows[kRows][kBwdPitch];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ ViewBlock sv;
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kBwdGroup;
+    const uint32_t g = g0 + lt;
+    const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
+    const bool vis = g < n && counts[g] != 0u;
+    if (lt == 0) mbar_init(&s_bar, 1);
+    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
+    const int any = __syncthreads_or(vis);
+    if (any) {
+        if (lt == 0) {
+            // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and
+            // spans a multiple of 256 bytes (g0 < n <= stride)
+            const uint32_t cols = min(kBwdGroup, stride - g0);
+            mbar_expect_tx(&s_bar, kRows * cols * 4u);
+            for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+        }
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0)) {
+            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
+                if (lt == 0 && status) atomicOr(status, kDevTimeout);
+                break;
+            }
+        }
+        if (vis) {
+            auto R_ = [&](int row) { return s_rows[row][lt]; };
+            auto W_ = [&](int row, float v) {
+                if (PACKED) s_rows[row][lt] = v;
+                else atomicAdd(out + (size_t)row * stride + g, v);
+            };
+            backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_);
+        } else if (PACKED) {
+            for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
+        }
+    }
+    if (!PACKED) return;
+    __syncthreads();
+    // the CTA's Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute block
+    struct Block { uint32_t row, width, base; };
+    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
+                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
+#pragma unroll
+    for (int bi = 0; bi < 6; ++bi) {
+        const Block bk = blocks[bi];
+        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
+        const uint32_t total = bk.width * cnt;
+        for (uint32_t i = lt; i < total; i += kBwdGroup)
+            dst[i] = any ? s_rows[bk.row + i % bk.width][i / bk.width] : 0.0f;
+    }
+}
+
 template <int TILE>
 void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
                      const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
@@ -490,12 +509,14 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
 }
 
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
+                                const uint32_t* counts, const float* grad2d, float* out, bool packed,
                                 uint32_t* status, cudaStream_t s) {
     if (n == 0) return;
-    k_preprocess_backward<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, 0, s>>>(rows, stride, n, view, counts,
-                                                                                grad2d, grows, accumulate ? 1 : 0,
-                                                                                status);
+    const uint32_t grid = (n + kBwdGroup - 1u) / kBwdGroup;
+    if (packed)
+        k_preprocess_backward<true><<<grid, kBwdGroup, 0, s>>>(rows, stride, n, view, counts, grad2d, out, status);
+    else
+        k_preprocess_backward<false><<<grid, kBwdGroup, 0, s>>>(rows, stride, n, view, counts, grad2d, out, status);
 }
 
 }  // namespace gs

@@ -259,7 +259,7 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 //   - keys/values are staged in shared memory in local sorted order and written out at
 //     global_digit_base + rank, which keeps runs of equal digits contiguous in global memory.
 template <int BITS>
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __restrict__ keys_in,
+__global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __restrict__ keys_in,
                                                            const uint32_t* __restrict__ vals_in,
                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                            const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
@@ -346,27 +346,39 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
         const uint32_t dstart = block_exclusive_scan<kSortThreads>(tid < RADIX ? cta_total : 0u, s_warp, &dtot);
         if (tid < RADIX) {
             s_dstart[tid] = dstart;
-            // serial lookback per digit (one thread per digit, bounded waits)
+            // lookback per digit (one thread per digit, bounded waits): the words of the next
+            // kLookWidth predecessors are loaded together, so a walk over partitions that have only
+            // published aggregates costs one memory round trip per kLookWidth steps
             uint32_t excl = 0;
             if (part != 0) {
+                constexpr int kLookWidth = 4;
                 int64_t j = (int64_t)part - 1;
                 const uint32_t want = seq & kSeqMask;
-                while (j >= 0) {
-                    const uint64_t* p = flags + (size_t)j * RADIX + tid;
-                    uint64_t w = ld_relaxed_u64(p);
-                    uint32_t spins = 0;
-                    while (word_seq(w) != want || word_flag(w) == 0u) {
-                        if (++spins > kSpinLimit) {
-                            atomicOr(&ctl->status, kDevTimeout);
-                            w = make_word(want, kFlagInclusive, 0u);
-                            break;
+                bool found = false;
+                while (!found && j >= 0) {
+                    uint64_t w[kLookWidth];
+#pragma unroll
+                    for (int q = 0; q < kLookWidth; ++q)
+                        w[q] = j - q >= 0 ? ld_relaxed_u64(flags + (size_t)(j - q) * RADIX + tid) : 0ull;
+#pragma unroll
+                    for (int q = 0; q < kLookWidth; ++q) {
+                        if (found || j - q < 0) break;
+                        const uint64_t* p = flags + (size_t)(j - q) * RADIX + tid;
+                        uint64_t v = w[q];
+                        uint32_t spins = 0;
+                        while (word_seq(v) != want || word_flag(v) == 0u) {
+                            if (++spins > kSpinLimit) {
+                                atomicOr(&ctl->status, kDevTimeout);
+                                v = make_word(want, kFlagInclusive, 0u);
+                                break;
+                            }
+                            if (spins > 64u) __nanosleep(64);
+                            v = ld_relaxed_u64(p);
                         }
-                        if (spins > 64u) __nanosleep(64);
-                        w = ld_relaxed_u64(p);
+                        excl += word_value(v);
+                        found = word_flag(v) == kFlagInclusive;
                     }
-                    excl += word_value(w);
-                    if (word_flag(w) == kFlagInclusive) break;
-                    --j;
+                    j -= kLookWidth;
                 }
                 st_relaxed_u64(flags + (size_t)part * RADIX + tid, make_word(seq, kFlagInclusive, excl + cta_total));
             }
@@ -455,6 +467,12 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     k_digit_hist<<<blocks, 256, 0, s>>>(keys, n, digit_bits, key_bits, hist);
+}
+
+void configure_sort_kernels() {
+    // the largest shared-memory carveout lets more onesweep CTAs (41 KB each) share an SM
+    cudaFuncSetAttribute(k_onesweep<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

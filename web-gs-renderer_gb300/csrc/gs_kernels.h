@@ -37,6 +37,8 @@ void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uin
 constexpr uint32_t kSortThreads = 256;
 constexpr uint32_t kSortItems = 16;
 constexpr uint32_t kSortPartition = kSortThreads * kSortItems;
+// Per-device kernel attributes (shared-memory carveout of the sort); call once per context.
+void configure_sort_kernels();
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
@@ -72,10 +74,11 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
                             const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
                             const float* dl_drgb, float* grad2d, cudaStream_t s);
-// grad2d -> dL/d(attribute rows), one thread per Gaussian, rows laid out like the scene.
-// accumulate: add into grows with FP32 atomics (several views of one scene) instead of storing.
+// grad2d -> dL/d(attributes), one thread per Gaussian.
+// packed: store into `out` in the packed input layout (59*n floats, zeros for invisible Gaussians);
+// else: add into 59 rows of `stride` floats with FP32 atomics (several views of one scene).
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* grows, bool accumulate,
+                                const uint32_t* counts, const float* grad2d, float* out, bool packed,
                                 uint32_t* status, cudaStream_t s);
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------

@@ -14,11 +14,10 @@
 //  * cut-off: a pixel whose power is below the splat's cut-off c_o = ln((1/255)/o) - 1e-3 skips
 //    the exp, since o*exp(power) < 1/255 is certain there (the 1e-3 margin is far beyond the
 //    rounding of exp, the product and logf);
-//  * warp cull: when staging a splat, the CTA computes its cull shape for the tile (a bounding box of
-//    the region where power >= c_o can hold, and the data of an exact ellipse-versus-rectangle
-//    test; gs_raster_common.cuh gives the bounds). Every warp tests its 8x4 pixel block against the
-//    32 splats of a group in parallel (one splat per lane, one ballot) and walks only the splats
-//    that meet its block, in range order. A skipped splat would have been rejected by every pixel
+//  * warp cull: when staging a splat, the CTA computes the bounding box of the region of the tile
+//    where power >= c_o can hold (gs_raster_common.cuh gives the bound). Every warp tests its 8x4
+//    pixel block against the 32 boxes of a group in parallel (one box per lane, one ballot) and
+//    walks only the splats whose box meets its block, in range order. A skipped splat would have been rejected by every pixel
 //    of the warp at "power < c_o" (or "power > 0"). Contributor counts are range positions, so
 //    skipping does not change them.
 #include "gs_kernels.h"
@@ -39,7 +38,6 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
     __shared__ float4 s_b[BATCH];    // (conic.z, opacity, r, g)
     __shared__ float2 s_c[BATCH];    // (b, cut)
     __shared__ float4 s_box[BATCH];  // cull box (x0, x1, y0, y1)
-    __shared__ float4 s_ell[BATCH];  // ellipse test data
 
     const uint32_t tile = blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
@@ -72,9 +70,7 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
                     s_a[j] = r0;
                     s_b[j] = r1;
                     s_c[j] = make_float2(r2.x, r2.y);
-                    const CullShape cs = cull_shape(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
-                    s_box[j] = cs.box;
-                    s_ell[j] = cs.ell;
+                    s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
                 } else {  // only after a timed-out sort: a splat that never blends
                     const float inf = __int_as_float(0x7f800000);
                     s_a[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -90,8 +86,7 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
         for (uint32_t g0 = 0; g0 < cnt; g0 += 32u) {
             if (__all_sync(0xffffffffu, done)) break;
             bool hit = false;
-            if (g0 + lane < cnt)
-                hit = block_meets(s_box[g0 + lane], s_ell[g0 + lane], s_a[g0 + lane], rx0, rx1, ry0, ry1);
+            if (g0 + lane < cnt) hit = box_meets(s_box[g0 + lane], rx0, rx1, ry0, ry1);
             uint32_t m = __ballot_sync(0xffffffffu, hit);
             while (m) {
                 const uint32_t j = g0 + (uint32_t)(__ffs(m) - 1);

@@ -4,21 +4,11 @@
 // Cull. For a splat with conic (a, b, c) and cut-off c_o = ln((1/255)/o) - 1e-3, a pixel can only
 // pass "power >= c_o" where Q(d) = a dx^2 + 2b dx dy + c dy^2 <= K', K' = -2 c_o plus the worst
 // rounding error of the pinned power formula anywhere in the tile (16 eps times S_max, the sum of
-// the absolute terms bounded over the tile). Two tests against a warp's pixel block, both
-// conservative, are applied in order:
-//  1. the bounding box of {Q <= K'} (det = ac - b^2 taken at its lower rounding bound) meets the
-//     block;
-//  2. the minimum of Q over the block's rectangle is at most K'. Q is convex, so with its centre
-//     outside the rectangle the minimum lies on an edge that faces the centre; the test evaluates
-//     one vertical and one horizontal edge (the facing ones; an edge that does not face the centre
-//     only adds a value >= the minimum), each at its clamped 1-D minimiser v = -b u / c (u = -b v /
-//     a). The signs of the rounded offsets equal the exact ones (a difference of two floats rounds
-//     to zero only when they are equal), so "centre inside" is decided exactly. The computed
-//     minimum is within 9 eps S_max of the exact one (edge offsets 2, the minimiser 2, the
-//     evaluation 5); the threshold adds 2^-17 S_max = 128 eps S_max and a relative 2^-16.
-// A splat that fails either test would have been rejected by every pixel of the block at
-// "power < c_o" (or "power > 0"), so skipping it changes no output bit. Splats whose shape cannot be
-// bounded safely (non-positive-definite or non-finite values) are never culled.
+// the absolute terms bounded over the tile). The cull box is the bounding box of {Q <= K'}, with
+// det = ac - b^2 taken at its lower rounding bound. A splat whose box misses a warp's pixel block
+// would have been rejected by every pixel of the block at "power < c_o" (or "power > 0"), so
+// skipping it changes no output bit. Splats whose box cannot be bounded safely (non-positive-definite
+// or non-finite values) are never culled.
 #pragma once
 #include "gs_common.cuh"
 
@@ -46,60 +36,32 @@ __device__ __forceinline__ float raster_expf(float x) {
 
 __device__ __forceinline__ bool finite_f(float v) { return fabsf(v) <= 3.0e38f; }
 
-// Cull data of one staged splat for one tile [tx0,tx1] x [ty0,ty1]:
-//   box = (x0, x1, y0, y1): (+inf, -inf, +inf, -inf) when no pixel can pass, (-inf, +inf, -inf,
-//         +inf) when no safe bound exists;
-//   ell = (threshold on the computed edge minimum of Q, -b/a, -b/c, c); threshold +inf when
-//         test 2 must keep the splat.
-struct CullShape {
-    float4 box;
-    float4 ell;
-};
-
-__device__ __forceinline__ CullShape cull_shape(float x, float y, float a, float b, float c, float cut, float tx0,
-                                                float tx1, float ty0, float ty1) {
+// Conservative box (x0, x1, y0, y1) for the tile [tx0,tx1] x [ty0,ty1]: (+inf, -inf, +inf, -inf)
+// when no pixel can pass, (-inf, +inf, -inf, +inf) when no safe bound exists.
+__device__ __forceinline__ float4 cull_box(float x, float y, float a, float b, float c, float cut, float tx0,
+                                           float tx1, float ty0, float ty1) {
     const float inf = __int_as_float(0x7f800000);
-    CullShape s;
-    s.box = make_float4(-inf, inf, -inf, inf);
-    s.ell = make_float4(inf, 0.0f, 0.0f, 0.0f);
-    if (!(finite_f(x) && finite_f(y) && finite_f(a) && finite_f(b) && finite_f(c)) || cut != cut) return s;
-    if (!(a > 0.0f) || !(c > 0.0f)) return s;
+    const float4 keep_all = make_float4(-inf, inf, -inf, inf);
+    if (!(finite_f(x) && finite_f(y) && finite_f(a) && finite_f(b) && finite_f(c)) || cut != cut) return keep_all;
+    if (!(a > 0.0f) || !(c > 0.0f)) return keep_all;
     const float dxm = fmaxf(fabsf(x - tx0), fabsf(x - tx1));
     const float dym = fmaxf(fabsf(y - ty0), fabsf(y - ty1));
     const float smax = (a * dxm * dxm + c * dym * dym + 2.0f * fabsf(b) * dxm * dym) * 1.01f;
-    if (!finite_f(smax)) return s;
-    if (cut > 0.0f) {  // power <= 0 < cut everywhere
-        s.box = make_float4(inf, -inf, inf, -inf);
-        return s;
-    }
+    if (!finite_f(smax)) return keep_all;
+    if (cut > 0.0f) return make_float4(inf, -inf, inf, -inf);  // power <= 0 < cut everywhere
     const float ac = a * c, bb = b * b;
     const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
-    if (!(det_lo > 0.0f)) return s;
+    if (!(det_lo > 0.0f)) return keep_all;
     const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
     const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
     const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
-    if (!finite_f(hx) || !finite_f(hy)) return s;
-    s.box = make_float4(x - hx, x + hx, y - hy, y + hy);
-    const float thr = k * (1.0f + 0x1p-16f) + 0x1p-17f * smax;
-    if (finite_f(thr)) s.ell = make_float4(thr, -b / a, -b / c, c);
-    return s;
+    if (!finite_f(hx) || !finite_f(hy)) return keep_all;
+    return make_float4(x - hx, x + hx, y - hy, y + hy);
 }
 
-// Test 1 then test 2 for the pixel block [rx0,rx1] x [ry0,ry1] (a sub-rectangle of the tile the
-// shape was made for); xyab = (x, y, a, b) as given to cull_shape.
-__device__ __forceinline__ bool block_meets(const float4& box, const float4& ell, const float4& xyab, float rx0,
-                                            float rx1, float ry0, float ry1) {
-    if (!(box.y >= rx0 && box.x <= rx1 && box.w >= ry0 && box.z <= ry1)) return false;
-    const float x = xyab.x, y = xyab.y, a = xyab.z, b = xyab.w, c = ell.w;
-    const float u0 = rx0 - x, u1 = rx1 - x, v0 = ry0 - y, v1 = ry1 - y;
-    if (u0 <= 0.0f && u1 >= 0.0f && v0 <= 0.0f && v1 >= 0.0f) return true;  // centre inside the block
-    const float ue = u0 > 0.0f ? u0 : u1;
-    const float ve = v0 > 0.0f ? v0 : v1;
-    const float vv = fminf(fmaxf(ell.z * ue, v0), v1);
-    const float uu = fminf(fmaxf(ell.y * ve, u0), u1);
-    const float qa = (a * ue) * ue + 2.0f * ((b * ue) * vv) + (c * vv) * vv;
-    const float qb = (a * uu) * uu + 2.0f * ((b * uu) * ve) + (c * ve) * ve;
-    return !(fminf(qa, qb) > ell.x);
+// Whether the box meets the pixel block [rx0,rx1] x [ry0,ry1].
+__device__ __forceinline__ bool box_meets(const float4& box, float rx0, float rx1, float ry0, float ry1) {
+    return box.y >= rx0 && box.x <= rx1 && box.w >= ry0 && box.z <= ry1;
 }
 
 }  // namespace gs
