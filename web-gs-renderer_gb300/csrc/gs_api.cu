@@ -279,7 +279,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
     cudaMemsetAsync(f.ranges.p, 0, (size_t)a.tiles_x * a.tiles_y * 2 * sizeof(uint32_t), s);
-    launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, 0, s);
+    launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, a.max_instance, 0, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
     launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,
                   a.tiles_x, a.tiles_y, a.out, s);

@@ -413,7 +413,8 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
     W_(kRowQuat + 3, (gq[2] - q[2] * qd) / qlen);
 }
 
-// One thread per Gaussian. A CTA with at least one visible Gaussian stages its 128-Gaussian slice of
+// One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
+// residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of
 // the 59 attribute rows in shared memory with bulk copies on one mbarrier (as the forward preprocess
 // does), so all of its loads are in flight at once.
 //   PACKED  the gradients replace the staged attributes in shared memory and the CTA writes its
@@ -422,7 +423,7 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
 //   !PACKED the gradients are added with FP32 atomics into 59 rows of `stride` floats (several views
 //           of one scene accumulate there; invisible Gaussians add nothing).
 template <bool PACKED>
-__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
+__global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
                                                                    uint32_t n, const ViewBlock* __restrict__ vb,
                                                                    const uint32_t* __restrict__ counts,
                                                                    const float* __restrict__ grad2d,

@@ -64,14 +64,15 @@ __global__ void k_frame_begin(FrameCtl* ctl) {
 // ---- fused offset scan + emit ---------------------------------------------------------------
 // Partition p covers entries [p*2048, p*2048+2048) of counts[0..n] (n+1 entries; counts[n] = 0).
 // 1. each thread loads 8 consecutive counts (two 16-byte loads), the block scans them;
-// 2. warp 0 publishes the partition aggregate and looks back for its exclusive prefix;
+// 2. the partition publishes its aggregate and sums its predecessors' aggregates in parallel;
 // 3. offsets[g] are written (offsets[n] = I), the partition holding entry n publishes I and
 //    min(I, max_instance) to FrameCtl (indirect_arg.wgsl:14-27);
 // 4. the partition's instances [excl, excl + total) are emitted by all 256 threads in slot order,
 //    each slot finding its Gaussian by binary search over the partition's local offsets, so one
 //    large splat never serialises a warp; keys are ((ty*tilesPerRow + tx) << 16) | depth16 in
 //    row-major tile order (emit.wgsl:55-66) and slots >= max_instance are dropped (:57-59);
-// 5. the digit histograms of every sort pass are accumulated on the fly.
+// 5. the digit histograms of every sort pass are accumulated on the fly (per Gaussian for the
+//    depth digits, per instance for the tile digits).
 __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __restrict__ counts,
                                                             const uint4* __restrict__ meta, uint32_t n,
                                                             uint32_t tiles_x, uint32_t max_instance,
@@ -117,15 +118,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
     uint32_t total;
     const uint32_t texcl = block_exclusive_scan<kScanThreads>(tsum, s_warp, &total);
 
-    // publish the aggregate, then look back for the exclusive prefix
-    if (tid < 32) {
-        if (tid == 0) st_relaxed_u64(flags + part, make_word(seq, part == 0 ? kFlagInclusive : kFlagAggregate, total));
-        const uint32_t excl = warp_lookback(flags, part, seq, &ctl->status);
-        if (tid == 0) {
-            if (part != 0) st_relaxed_u64(flags + part, make_word(seq, kFlagInclusive, excl + total));
-            s_excl = excl;
-        }
-    }
+    // publish the aggregate at once; the local offsets and rects are staged while predecessors do
+    // the same
+    if (tid == 0) st_relaxed_u64(flags + part, make_word(seq, kFlagAggregate, total));
     // local offsets and rects into shared memory
     {
         uint32_t run = texcl;
@@ -141,6 +136,31 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
             run += c[k];
         }
         if (tid == 0) s_off[kScanPartition] = total;
+    }
+    // sum the aggregates of all predecessors: every partition publishes before it waits on anything
+    // and its predecessors hold smaller tickets (they are running or done), so the waits end without
+    // a chain of inclusive prefixes; one word per thread per 256 predecessors is read
+    {
+        const uint32_t want = seq & kSeqMask;
+        uint32_t psum = 0;
+        for (uint32_t j = tid; j < part; j += kScanThreads) {
+            const uint64_t* p = flags + j;
+            uint64_t w = ld_relaxed_u64(p);
+            uint32_t spins = 0;
+            while (word_seq(w) != want || word_flag(w) == 0u) {
+                if (++spins > kSpinLimit) {  // bounded: record the timeout and count the partition as empty
+                    atomicOr(&ctl->status, kDevTimeout);
+                    w = make_word(want, kFlagAggregate, 0u);
+                    break;
+                }
+                if (spins > 64u) __nanosleep(64);
+                w = ld_relaxed_u64(p);
+            }
+            psum += word_value(w);
+        }
+        uint32_t excl_sum;
+        block_exclusive_scan<kScanThreads>(psum, s_warp, &excl_sum);
+        if (tid == 0) s_excl = excl_sum;
     }
     if (vis) atomicAdd(&ctl->visible, vis);
     __syncthreads();
@@ -159,8 +179,23 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
         }
     }
 
-    // emit
+    // digits of the depth bits depend on the Gaussian only: one histogram add per Gaussian, weighted
+    // by its kept instances (slots below max_instance); the tile digits are counted per instance
     const uint32_t mask = radix - 1u;
+    const uint32_t depth_passes = min(passes, 16u / digit_bits);
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        const uint32_t lg = tid * kScanItems + k;
+        if (c[k] == 0u) continue;
+        const uint32_t first = excl + s_off[lg];
+        const uint32_t kept = first >= max_instance ? 0u : min(c[k], max_instance - first);
+        if (kept == 0u) continue;
+        const uint32_t d16 = s_depth[lg];
+        for (uint32_t p = 0; p < depth_passes; ++p)
+            atomicAdd(&s_hist[p * radix + ((d16 >> (p * digit_bits)) & mask)], kept);
+    }
+
+    // emit
     for (uint32_t i = tid; i < total; i += kScanThreads) {
         const uint32_t slot_i = excl + i;
         if (slot_i >= max_instance) break;
@@ -178,7 +213,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
         const uint32_t key = ((ty * tiles_x + tx) << 16u) | s_depth[lo];
         keys[slot_i] = key;
         vals[slot_i] = base + lo;
-        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+        for (uint32_t p = depth_passes; p < passes; ++p)
+            atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
     }
     __syncthreads();
     for (uint32_t i = tid; i < passes * radix; i += kScanThreads)
@@ -411,23 +447,40 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
 }
 
 // ---- tile ranges (tile_ranges.wgsl:7-34) over the sorted prefix -----------------------------------
-// Tiles outside [0, tiles) can only come from a timed-out sort; they are skipped.
+// Each thread takes four consecutive keys (one 16-byte load) and the key before them, so every load
+// of the pass is independent and in flight at once. Tiles outside [0, tiles) can only come from a
+// timed-out sort; they are skipped.
 __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCtl* ctl, uint32_t tiles,
                               uint32_t* __restrict__ ranges) {
     const uint32_t n = ctl->sorted_count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t tile = keys[i] >> 16u;
-        if (tile >= tiles) continue;
-        if (i == 0u) {
-            ranges[tile * 2u] = 0u;
+    const uint32_t quads = (n + 3u) / 4u;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += gridDim.x * blockDim.x) {
+        const uint32_t i0 = q * 4u;
+        uint32_t k[4];
+        if (i0 + 4u <= n) {
+            const uint4 v = reinterpret_cast<const uint4*>(keys)[q];
+            k[0] = v.x; k[1] = v.y; k[2] = v.z; k[3] = v.w;
         } else {
-            const uint32_t prev = keys[i - 1u] >> 16u;
-            if (tile > prev && prev < tiles) {
-                ranges[prev * 2u + 1u] = i;
-                ranges[tile * 2u] = i;
-            }
+#pragma unroll
+            for (uint32_t j = 0; j < 4u; ++j) k[j] = i0 + j < n ? keys[i0 + j] : 0u;
         }
-        if (i == n - 1u) ranges[tile * 2u + 1u] = n;
+        uint32_t prev = i0 ? keys[i0 - 1u] >> 16u : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < 4u; ++j) {
+            const uint32_t i = i0 + j;
+            if (i >= n) break;
+            const uint32_t tile = k[j] >> 16u;
+            if (tile < tiles) {
+                if (i == 0u) {
+                    ranges[tile * 2u] = 0u;
+                } else if (tile > prev && prev < tiles) {
+                    ranges[prev * 2u + 1u] = i;
+                    ranges[tile * 2u] = i;
+                }
+                if (i == n - 1u) ranges[tile * 2u + 1u] = n;
+            }
+            prev = tile;
+        }
     }
 }
 
@@ -491,9 +544,13 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
                                                      hist, ctl, flags, slot);
 }
 
-void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,
-                        cudaStream_t s) {
-    const uint32_t grid = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
+void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
+                        int grid_cap, cudaStream_t s) {
+    // one quad of keys per thread up to max_n keys, at most 16 CTAs per SM (grid-stride beyond)
+    uint32_t grid = (max_n / 4u + 255u) / 256u;
+    const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 16u;
+    if (grid > cap) grid = cap;
+    if (grid == 0) grid = 1;
     k_tile_ranges<<<grid, 256, 0, s>>>(keys, ctl, tiles, ranges);
 }
 

@@ -51,8 +51,8 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
                            uint32_t slot, cudaStream_t s, uint32_t grid = 0);
 
-void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, int grid_cap,
-                        cudaStream_t s);
+void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
+                        int grid_cap, cudaStream_t s);
 
 struct RasterOut {
     uint32_t* rgba8;     // W*H packed rgba8 or null

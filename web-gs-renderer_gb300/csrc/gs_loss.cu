@@ -7,7 +7,9 @@
 // halo staged in shared memory (both separable passes happen there):
 //   k_ssim_fwd  moments -> SSIM map -> its three partials (to global) + per-block SSIM and L1 sums;
 //   k_ssim_bwd  blurred partials + the L1 term -> dL/dx.
-// Images are H x W x 3 (pixel-interleaved).
+// Images are H x W x 3 (pixel-interleaved). The library is compiled without multiply-add
+// contraction (the splat kernels need it so); the loss is not bit-pinned, so its filters use
+// explicit fused multiply-adds.
 #include <cmath>
 
 #include "gs_kernels.h"
@@ -19,72 +21,110 @@ struct Window {
     float w[11];
 };
 
-constexpr int kTX = 32, kTY = 16, kR = 5;
-constexpr int kHX = kTX + 2 * kR, kHY = kTY + 2 * kR;  // haloed tile
+constexpr int kT = 32;              // output tile (kT x kT pixels of one channel)
+constexpr int kR = 5;               // window radius
+constexpr int kH = kT + 2 * kR;     // haloed tile edge (42)
+constexpr int kPitchIn = kH + 1;    // 43: the horizontal pass reads rows conflict-free
+constexpr int kPitchH = kT + 1;     // 33
+constexpr int kThreads = 256;
+constexpr int kRunH = 8;            // horizontal pass: 8 consecutive outputs of one row per thread
+constexpr int kItemsH = kH * (kT / kRunH);  // 168 row runs
+constexpr int kRunV = 4;            // vertical pass: 4 consecutive outputs of one column per thread
+static_assert(kT * (kT / kRunV) == kThreads, "one vertical run per thread");
 
-__global__ void __launch_bounds__(kTX * kTY) k_ssim_fwd(const float* __restrict__ x, const float* __restrict__ y,
-                                                        uint32_t W, uint32_t H, Window win,
-                                                        float* __restrict__ partial /* 9 planes */,
-                                                        double* __restrict__ block_sums) {
-    __shared__ float sx[kHY][kHX], sy[kHY][kHX];
-    __shared__ float hm[5][kHY][kTX];
-    __shared__ float red[2][kTX * kTY / 32];
+// Stages rows [ty0, ty0 + kH) x cols [tx0, tx0 + kH) of channel ch of an H x W x 3 image (zeros
+// outside) into dst (pitch kPitchIn).
+__device__ __forceinline__ void stage_channel(const float* __restrict__ img, uint32_t W, uint32_t H, int tx0,
+                                              int ty0, int ch, float* dst) {
+    for (int i = threadIdx.x; i < kH * kH; i += kThreads) {
+        const int ly = i / kH, lx = i - ly * kH, gx = tx0 + lx, gy = ty0 + ly;
+        float v = 0.0f;
+        if (gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H) v = img[((size_t)gy * W + gx) * 3 + ch];
+        dst[ly * kPitchIn + lx] = v;
+    }
+}
+
+// Moments of x and y over the window, the SSIM map, its partials with respect to the moments, and
+// per-block sums of SSIM and |x - y|. Each thread filters a run of 8 outputs of one row (the 18 inputs
+// it needs stay in registers), then a run of 4 outputs of one column.
+__global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__ x, const float* __restrict__ y,
+                                                       uint32_t W, uint32_t H, Window win,
+                                                       float* __restrict__ partial /* 9 planes */,
+                                                       double* __restrict__ block_sums) {
+    __shared__ float sx[kH * kPitchIn], sy[kH * kPitchIn];
+    __shared__ float hm[5][kH * kPitchH];
+    __shared__ float red[2][kThreads / 32];
     const int ch = blockIdx.z;
-    const int tx0 = blockIdx.x * kTX - kR, ty0 = blockIdx.y * kTY - kR;
-    const int tid = threadIdx.y * kTX + threadIdx.x;
-    for (int i = tid; i < kHX * kHY; i += kTX * kTY) {
-        const int lx = i % kHX, ly = i / kHX, gx = tx0 + lx, gy = ty0 + ly;
-        float a = 0.0f, b = 0.0f;
-        if (gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H) {
-            const size_t q = ((size_t)gy * W + gx) * 3 + ch;
-            a = x[q];
-            b = y[q];
-        }
-        sx[ly][lx] = a;
-        sy[ly][lx] = b;
-    }
+    const int tx0 = blockIdx.x * kT - kR, ty0 = blockIdx.y * kT - kR;
+    const int tid = threadIdx.x;
+    stage_channel(x, W, H, tx0, ty0, ch, sx);
+    stage_channel(y, W, H, tx0, ty0, ch, sy);
     __syncthreads();
-    for (int i = tid; i < kTX * kHY; i += kTX * kTY) {  // horizontal pass over every haloed row
-        const int c = i % kTX, r = i / kTX;
-        float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+    if (tid < kItemsH) {
+        const int r = tid / (kT / kRunH), c0 = (tid % (kT / kRunH)) * kRunH;
+        float a[kRunH + 2 * kR], b[kRunH + 2 * kR];
 #pragma unroll
-        for (int k = 0; k < 11; ++k) {
-            const float a = sx[r][c + k], b = sy[r][c + k], w = win.w[k];
-            s0 += w * a;
-            s1 += w * b;
-            s2 += w * a * a;
-            s3 += w * b * b;
-            s4 += w * a * b;
+        for (int j = 0; j < kRunH + 2 * kR; ++j) {
+            a[j] = sx[r * kPitchIn + c0 + j];
+            b[j] = sy[r * kPitchIn + c0 + j];
         }
-        hm[0][r][c] = s0; hm[1][r][c] = s1; hm[2][r][c] = s2; hm[3][r][c] = s3; hm[4][r][c] = s4;
+#pragma unroll
+        for (int o = 0; o < kRunH; ++o) {
+            float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+#pragma unroll
+            for (int k = 0; k < 2 * kR + 1; ++k) {
+                const float av = a[o + k], bv = b[o + k], w = win.w[k];
+                const float wa = w * av, wb = w * bv;
+                s0 += wa;
+                s1 += wb;
+                s2 = fmaf(wa, av, s2);
+                s3 = fmaf(wb, bv, s3);
+                s4 = fmaf(wa, bv, s4);
+            }
+            const int q = r * kPitchH + c0 + o;
+            hm[0][q] = s0; hm[1][q] = s1; hm[2][q] = s2; hm[3][q] = s3; hm[4][q] = s4;
+        }
     }
     __syncthreads();
-    const int c = threadIdx.x, r = threadIdx.y;
-    const int gx = blockIdx.x * kTX + c, gy = blockIdx.y * kTY + r;
+    const int c = tid % kT, r0 = (tid / kT) * kRunV;
+    const int gx = blockIdx.x * kT + c;
+    float m[kRunV][5];
+#pragma unroll
+    for (int o = 0; o < kRunV; ++o)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) m[o][q] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        float v[kRunV + 2 * kR];
+#pragma unroll
+        for (int j = 0; j < kRunV + 2 * kR; ++j) v[j] = hm[q][(r0 + j) * kPitchH + c];
+#pragma unroll
+        for (int o = 0; o < kRunV; ++o)
+#pragma unroll
+            for (int k = 0; k < 2 * kR + 1; ++k) m[o][q] = fmaf(win.w[k], v[o + k], m[o][q]);
+    }
+    const size_t P = (size_t)W * H;
     float ssim = 0.0f, l1 = 0.0f;
-    if (gx < (int)W && gy < (int)H) {
-        float m[5] = {0, 0, 0, 0, 0};
 #pragma unroll
-        for (int k = 0; k < 11; ++k) {
-            const float w = win.w[k];
-#pragma unroll
-            for (int q = 0; q < 5; ++q) m[q] += w * hm[q][r + k][c];
-        }
+    for (int o = 0; o < kRunV; ++o) {
+        const int gy = blockIdx.y * kT + r0 + o;
+        if (gx >= (int)W || gy >= (int)H) continue;
         const float C1 = 0.01f * 0.01f, C2 = 0.03f * 0.03f;
-        const float mx = m[0], my = m[1];
-        const float sxx = m[2] - mx * mx, syy = m[3] - my * my, sxy = m[4] - mx * my;
+        const float mx = m[o][0], my = m[o][1];
+        const float sxx = m[o][2] - mx * mx, syy = m[o][3] - my * my, sxy = m[o][4] - mx * my;
         const float A1 = 2.0f * mx * my + C1, A2 = 2.0f * sxy + C2;
         const float B1 = mx * mx + my * my + C1, B2 = sxx + syy + C2;
-        const float s = A1 * A2 / (B1 * B2);
-        const float ds_dmx = (2.0f * my * A2) / (B1 * B2) - s * (2.0f * mx) / B1;
-        const float ds_dsxx = -s / B2;
-        const float ds_dsxy = 2.0f * A1 / (B1 * B2);
-        const size_t P = (size_t)W * H, o = (size_t)gy * W + gx;
-        partial[(ch * 3 + 0) * P + o] = ds_dmx + ds_dsxx * (-2.0f * mx) + ds_dsxy * (-my);
-        partial[(ch * 3 + 1) * P + o] = ds_dsxx;
-        partial[(ch * 3 + 2) * P + o] = ds_dsxy;
-        ssim = s;
-        l1 = fabsf(sx[r + kR][c + kR] - sy[r + kR][c + kR]);
+        const float inv_b = 1.0f / (B1 * B2);
+        const float sv = A1 * A2 * inv_b;
+        const float ds_dmx = (2.0f * my * A2) * inv_b - sv * (2.0f * mx) / B1;
+        const float ds_dsxx = -sv / B2;
+        const float ds_dsxy = 2.0f * A1 * inv_b;
+        const size_t po = (size_t)gy * W + gx;
+        partial[(ch * 3 + 0) * P + po] = ds_dmx + ds_dsxx * (-2.0f * mx) + ds_dsxy * (-my);
+        partial[(ch * 3 + 1) * P + po] = ds_dsxx;
+        partial[(ch * 3 + 2) * P + po] = ds_dsxy;
+        ssim += sv;
+        l1 += fabsf(sx[(r0 + o + kR) * kPitchIn + c + kR] - sy[(r0 + o + kR) * kPitchIn + c + kR]);
     }
     for (int k = 16; k > 0; k >>= 1) {
         ssim += __shfl_xor_sync(0xffffffffu, ssim, k);
@@ -94,65 +134,81 @@ __global__ void __launch_bounds__(kTX * kTY) k_ssim_fwd(const float* __restrict_
     if (lane == 0) { red[0][warp] = ssim; red[1][warp] = l1; }
     __syncthreads();
     if (warp == 0) {
-        constexpr int kWarps = kTX * kTY / 32;
-        float a = lane < kWarps ? red[0][lane] : 0.0f, b = lane < kWarps ? red[1][lane] : 0.0f;
+        constexpr int kWarps = kThreads / 32;
+        float s_ = lane < kWarps ? red[0][lane] : 0.0f, l_ = lane < kWarps ? red[1][lane] : 0.0f;
         for (int k = 16; k > 0; k >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, k);
-            b += __shfl_xor_sync(0xffffffffu, b, k);
+            s_ += __shfl_xor_sync(0xffffffffu, s_, k);
+            l_ += __shfl_xor_sync(0xffffffffu, l_, k);
         }
         if (lane == 0) {
             const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-            block_sums[2 * blk] = (double)a;
-            block_sums[2 * blk + 1] = (double)b;
+            block_sums[2 * blk] = (double)s_;
+            block_sums[2 * blk + 1] = (double)l_;
         }
     }
 }
 
-__global__ void __launch_bounds__(kTX * kTY) k_ssim_bwd(const float* __restrict__ partial, const float* __restrict__ x,
-                                                        const float* __restrict__ y, uint32_t W, uint32_t H,
-                                                        Window win, float lambda, float* __restrict__ dl) {
-    __shared__ float sp[3][kHY][kHX];
-    __shared__ float hp[3][kHY][kTX];
+// dL/dx from the blurred partials (same tiling and register blocking as k_ssim_fwd).
+__global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__ partial, const float* __restrict__ x,
+                                                       const float* __restrict__ y, uint32_t W, uint32_t H,
+                                                       Window win, float lambda, float* __restrict__ dl) {
+    __shared__ float sp[3][kH * kPitchIn];
+    __shared__ float hp[3][kH * kPitchH];
     const int ch = blockIdx.z;
-    const int tx0 = blockIdx.x * kTX - kR, ty0 = blockIdx.y * kTY - kR;
-    const int tid = threadIdx.y * kTX + threadIdx.x;
+    const int tx0 = blockIdx.x * kT - kR, ty0 = blockIdx.y * kT - kR;
+    const int tid = threadIdx.x;
     const size_t P = (size_t)W * H;
-    for (int i = tid; i < kHX * kHY; i += kTX * kTY) {
-        const int lx = i % kHX, ly = i / kHX, gx = tx0 + lx, gy = ty0 + ly;
+    for (int i = tid; i < kH * kH; i += kThreads) {
+        const int ly = i / kH, lx = i - ly * kH, gx = tx0 + lx, gy = ty0 + ly;
         const bool in = gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H;
         const size_t o = in ? (size_t)gy * W + gx : 0;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) sp[q][ly][lx] = in ? partial[(ch * 3 + q) * P + o] : 0.0f;
+        for (int q = 0; q < 3; ++q) sp[q][ly * kPitchIn + lx] = in ? partial[(ch * 3 + q) * P + o] : 0.0f;
     }
     __syncthreads();
-    for (int i = tid; i < kTX * kHY; i += kTX * kTY) {
-        const int c = i % kTX, r = i / kTX;
-        float s[3] = {0, 0, 0};
+    if (tid < kItemsH) {
+        const int r = tid / (kT / kRunH), c0 = (tid % (kT / kRunH)) * kRunH;
 #pragma unroll
-        for (int k = 0; k < 11; ++k) {
-            const float w = win.w[k];
+        for (int q = 0; q < 3; ++q) {
+            float v[kRunH + 2 * kR];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) s[q] += w * sp[q][r][c + k];
+            for (int j = 0; j < kRunH + 2 * kR; ++j) v[j] = sp[q][r * kPitchIn + c0 + j];
+#pragma unroll
+            for (int o = 0; o < kRunH; ++o) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 2 * kR + 1; ++k) acc = fmaf(win.w[k], v[o + k], acc);
+                hp[q][r * kPitchH + c0 + o] = acc;
+            }
         }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) hp[q][r][c] = s[q];
     }
     __syncthreads();
-    const int c = threadIdx.x, r = threadIdx.y;
-    const int gx = blockIdx.x * kTX + c, gy = blockIdx.y * kTY + r;
-    if (gx >= (int)W || gy >= (int)H) return;
-    float b[3] = {0, 0, 0};
+    const int c = tid % kT, r0 = (tid / kT) * kRunV;
+    const int gx = blockIdx.x * kT + c;
+    float bl[kRunV][3];
 #pragma unroll
-    for (int k = 0; k < 11; ++k) {
-        const float w = win.w[k];
+    for (int q = 0; q < 3; ++q) {
+        float v[kRunV + 2 * kR];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) b[q] += w * hp[q][r + k][c];
+        for (int j = 0; j < kRunV + 2 * kR; ++j) v[j] = hp[q][(r0 + j) * kPitchH + c];
+#pragma unroll
+        for (int o = 0; o < kRunV; ++o) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 2 * kR + 1; ++k) acc = fmaf(win.w[k], v[o + k], acc);
+            bl[o][q] = acc;
+        }
     }
-    const size_t q = ((size_t)gy * W + gx) * 3 + ch;
-    const float xv = x[q], yv = y[q], d = xv - yv;
     const float inv = 1.0f / (float)(3 * P);
-    const float g_l1 = (d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f));
-    dl[q] = g_l1 - lambda * inv * (b[0] + 2.0f * xv * b[1] + yv * b[2]);
+#pragma unroll
+    for (int o = 0; o < kRunV; ++o) {
+        const int gy = blockIdx.y * kT + r0 + o;
+        if (gx >= (int)W || gy >= (int)H) continue;
+        const size_t q = ((size_t)gy * W + gx) * 3 + ch;
+        const float xv = x[q], yv = y[q], d = xv - yv;
+        const float g_l1 = (d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f));
+        dl[q] = g_l1 - lambda * inv * (bl[o][0] + 2.0f * xv * bl[o][1] + yv * bl[o][2]);
+    }
 }
 
 // sums[0..1] = column sums of the per-block partials that follow them
@@ -198,7 +254,7 @@ Window make_window() {
 }
 
 dim3 loss_grid(uint32_t width, uint32_t height) {
-    return dim3((width + kTX - 1) / kTX, (height + kTY - 1) / kTY, 3);
+    return dim3((width + kT - 1) / kT, (height + kT - 1) / kT, 3);
 }
 
 }  // namespace
@@ -213,7 +269,7 @@ size_t loss_sum_doubles(uint32_t width, uint32_t height) {
 void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_t height, float lambda,
                          float* scratch, double* sums, float* dl, cudaStream_t s) {
     const Window win = make_window();
-    const dim3 grid = loss_grid(width, height), block(kTX, kTY);
+    const dim3 grid = loss_grid(width, height), block(kThreads);
     k_ssim_fwd<<<grid, block, 0, s>>>(x, y, width, height, win, scratch, sums + 2);
     k_reduce_sums<<<1, 1024, 0, s>>>(sums, (size_t)grid.x * grid.y * grid.z);
     if (dl) k_ssim_bwd<<<grid, block, 0, s>>>(scratch, x, y, width, height, win, lambda, dl);
