@@ -108,7 +108,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
 
 
-# ---- algorithmic bytes per pass (stated in the design doc) ----------------------------------------------------
+# ---- algorithmic bytes per pass ----------------------------------------------------------------------
 def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
     npass, vis, s = fi["near_pass"], fi["visible"], fi["sorted_count"]
     tiles = fi["tiles_x"] * fi["tiles_y"]
@@ -124,6 +124,16 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
         # per instance the index and the 48 B record, per tile its range, per pixel 4 B rgba8
         "raster": 52 * s + 8 * tiles + 4 * pixels,
     }
+
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu --set full capture of
+# the forward frame of this workload on a GB300) and what bounds each kernel there.
+NCU_TRAFFIC_BYTES = {"preprocess": 285.9e6, "raster": 54.6e6}
+LIMITER = {
+    "raster": "instruction issue (ncu: issue slots busy 89%, DRAM 2% of peak; the 48-byte records "
+              "are re-read from L2, so DRAM traffic is below the algorithmic bytes)",
+    "preprocess": "HBM (ncu: 58% of DRAM peak, stalls on the bulk-copy wait)",
+}
 
 
 def peaks() -> tuple[float, str]:
@@ -319,8 +329,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     peak, peak_kind = peaks()
     achieved = bytes_per[top] / (kernel_passes[top] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-            "algorithmic_bytes": int(bytes_per[top])}
+            "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get(top), "peak_source": peak_kind,
+            "algorithmic_bytes": int(bytes_per[top]), "limiter": LIMITER.get(top)}
     per_pass = {k: {"ms": round(v, 4), "bytes": int(bytes_per.get(k, 0)),
                     "GBps": round(bytes_per.get(k, 0) / (v * 1e-3) / 1e9, 1) if v > 0 and k in bytes_per else None}
                 for k, v in pass_ms.items()}
@@ -490,12 +500,24 @@ def batched_forward(steps, warmup, local_rank) -> dict:
         ms_plain = _timed(stream, plain, steps, warmup)
         ms_batch = _timed(stream, batch, steps, warmup)
         pix = sum(c.width * c.height for _, c in cams)
+        if label == "default":
+            # each view alone (graph-replayed frames): the large views bound what overlap can gain
+            per_view = []
+            for k, (si, c) in enumerate(cams):
+                def one(k=k, si=si):
+                    ctx.forward_device(scs[si], views[k], rgba8=imgs[k].data_ptr())
+                per_view.append({"scene": W.BATCH_SCENES[si].count, "res": f"{c.width}x{c.height}",
+                                 "ms": round(_timed(stream, one, max(5, steps // 2), warmup), 4)})
         res[label] = {"config": cfg or {"tile_size": 16, "digit_bits": 8, "raster_batch": 256},
                       "plain_ms_per_view": round(ms_plain / len(cams), 4),
                       "batched_ms_per_view": round(ms_batch / len(cams), 4),
                       "plain_Mpix_s": round(pix / ms_plain / 1e3, 1), "batched_Mpix_s": round(pix / ms_batch / 1e3, 1),
                       "batched_over_plain": round(ms_plain / ms_batch, 3)}
         if label == "default":
+            big = sum(v["ms"] for v in per_view if v["scene"] == max(s.count for s in W.BATCH_SCENES))
+            res[label]["per_view_plain"] = per_view
+            res[label]["largest_scene_views_ms"] = round(big, 4)
+            res[label]["overlap_bound_batched_over_plain"] = round(sum(v["ms"] for v in per_view) / big, 3)
             # end to end: every view's rgba8 image lands in pinned host memory; plain = one synchronous
             # gs_forward per view (one Renderer.execute() per view), batched = one gs_forward_batch
             hosts = [torch.empty(c.width * c.height * 4, dtype=torch.uint8, pin_memory=True) for _, c in cams]
