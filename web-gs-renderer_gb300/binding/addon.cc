@@ -1,13 +1,15 @@
 // addon.cc -- Node N-API binding of libwebgs.so for the reference's JavaScript Renderer.
 //
 // Exposes the C ABI of include/gs.h to JavaScript with the shape renderer.js uses: a native context
-// object with uploadGsData / setGs / execute / timings. Status codes become thrown JS Errors, the
+// object with uploadGsData / setGs / render / timings, plus the differentiable pair (renderRgb /
+// backward), the L1 + SSIM loss and the batched render. Status codes become thrown JS Errors, the
 // way the reference's fail() (src/utils/utils.js:3-47) throws. Source only in this repository: the
 // build image has no Node runtime or node_api.h.
 #include <node_api.h>
 
 #include <map>
 #include <string>
+#include <vector>
 
 #include "../../include/gs.h"
 
@@ -33,7 +35,7 @@ Native* unwrap(napi_env env, napi_callback_info info, size_t* argc, napi_value* 
     return n;
 }
 
-// new Native({tileSize, digitBits, rasterBatch, maxInstanceFactor, profile})
+// new Native({tileSize, digitBits, rasterBatch, maxInstanceFactor, profile, differentiable})
 napi_value construct(napi_env env, napi_callback_info info) {
     size_t argc = 1;
     napi_value argv[1], self;
@@ -54,6 +56,8 @@ napi_value construct(napi_env env, napi_callback_info info) {
         }
         napi_has_named_property(env, argv[0], "profile", &has);
         if (has) cfg.flags |= GS_FLAG_PROFILE;
+        napi_has_named_property(env, argv[0], "differentiable", &has);
+        if (has) cfg.flags |= GS_FLAG_DIFFERENTIABLE;
     }
     Native* n = new Native();
     const int rc = gs_ctx_create(&cfg, &n->ctx);
@@ -135,9 +139,147 @@ napi_value render(napi_env env, napi_callback_info info) {
     size_t length = 0;
     void* pixels = nullptr;
     napi_get_typedarray_info(env, argv[1], &type, &length, &pixels, nullptr, nullptr);
+    const gs_view* vb = static_cast<const gs_view*>(view);
+    if (type != napi_uint8_array || length != (size_t)vb->texture_size[0] * vb->texture_size[1] * 4) {
+        napi_throw_type_error(env, nullptr, "image must be a Uint8Array of W*H*4 bytes");
+        return nullptr;
+    }
     gs_image img{GS_MEM_HOST, static_cast<uint8_t*>(pixels), nullptr, nullptr, nullptr};
     const int rc = gs_forward(n->ctx, it->second, static_cast<const gs_view*>(view), &img);
     if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return throw_status(env, rc, n->ctx);  // overflow truncates silently
+    return nullptr;
+}
+
+// Float32Array argument i of exactly `count` floats, or a thrown TypeError.
+float* float_array(napi_env env, napi_value v, size_t count, const char* what) {
+    napi_typedarray_type type;
+    size_t length = 0;
+    void* data = nullptr;
+    if (napi_get_typedarray_info(env, v, &type, &length, &data, nullptr, nullptr) != napi_ok ||
+        type != napi_float32_array || length != count) {
+        napi_throw_type_error(env, nullptr, (std::string(what) + ": wrong Float32Array length").c_str());
+        return nullptr;
+    }
+    return static_cast<float*>(data);
+}
+
+const gs_view* view_block(napi_env env, napi_value v) {
+    void* view = nullptr;
+    size_t vlen = 0;
+    if (napi_get_arraybuffer_info(env, v, &view, &vlen) != napi_ok || vlen != sizeof(gs_view)) {
+        napi_throw_type_error(env, nullptr, "view block must be a 176-byte ArrayBuffer");
+        return nullptr;
+    }
+    return static_cast<const gs_view*>(view);
+}
+
+// renderRgb(viewBlock, rgb: Float32Array(W*H*3)) -- the forward of the differentiable op: fp32 colour
+// before quantization; with {differentiable: true} the context keeps what backward needs
+napi_value render_rgb(napi_env env, napi_callback_info info) {
+    size_t argc = 2;
+    napi_value argv[2];
+    Native* n = unwrap(env, info, &argc, argv);
+    auto it = n->scenes.find(n->current);
+    if (it == n->scenes.end()) return nullptr;
+    const gs_view* view = view_block(env, argv[0]);
+    if (!view) return nullptr;
+    const size_t pix = (size_t)view->texture_size[0] * view->texture_size[1];
+    float* rgb = float_array(env, argv[1], pix * 3, "rgb");
+    if (!rgb) return nullptr;
+    gs_image img{GS_MEM_HOST, nullptr, rgb, nullptr, nullptr};
+    const int rc = gs_forward(n->ctx, it->second, view, &img);
+    if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return throw_status(env, rc, n->ctx);
+    return nullptr;
+}
+
+// backward(dLdRgb: Float32Array(W*H*3), grad: Float32Array(59*count)) -- gradients of the last
+// renderRgb with respect to the packed attributes (the uploadGsData layout)
+napi_value backward(napi_env env, napi_callback_info info) {
+    size_t argc = 2;
+    napi_value argv[2];
+    Native* n = unwrap(env, info, &argc, argv);
+    auto it = n->scenes.find(n->current);
+    if (it == n->scenes.end()) {
+        napi_throw_error(env, nullptr, "backward: no scene selected");
+        return nullptr;
+    }
+    napi_typedarray_type type;
+    size_t dl_len = 0;
+    void* dl = nullptr;
+    napi_get_typedarray_info(env, argv[0], &type, &dl_len, &dl, nullptr, nullptr);
+    if (type != napi_float32_array) {
+        napi_throw_type_error(env, nullptr, "dLdRgb must be a Float32Array");
+        return nullptr;
+    }
+    float* grad = float_array(env, argv[1], (size_t)gs_scene_count(it->second) * 59, "grad");
+    if (!grad) return nullptr;
+    const int rc = gs_backward(n->ctx, it->second, static_cast<const float*>(dl), grad, GS_MEM_HOST);
+    if (rc != GS_OK) return throw_status(env, rc, n->ctx);
+    return nullptr;
+}
+
+// loss(rgb, target, width, height, lambda, dLdRgb) -> L1 + lambda (1 - SSIM); dLdRgb receives dL/drgb
+napi_value loss(napi_env env, napi_callback_info info) {
+    size_t argc = 6;
+    napi_value argv[6];
+    Native* n = unwrap(env, info, &argc, argv);
+    uint32_t w = 0, h = 0;
+    double lambda = 0.2;
+    napi_get_value_uint32(env, argv[2], &w);
+    napi_get_value_uint32(env, argv[3], &h);
+    napi_get_value_double(env, argv[4], &lambda);
+    const size_t count = (size_t)w * h * 3;
+    float* rgb = float_array(env, argv[0], count, "rgb");
+    float* target = rgb ? float_array(env, argv[1], count, "target") : nullptr;
+    float* dl = target ? float_array(env, argv[5], count, "dLdRgb") : nullptr;
+    if (!dl) return nullptr;
+    double value = 0.0;
+    const int rc = gs_loss_l1_ssim(n->ctx, rgb, target, w, h, (float)lambda, &value, dl, GS_MEM_HOST);
+    if (rc != GS_OK) return throw_status(env, rc, n->ctx);
+    napi_value out;
+    napi_create_double(env, value, &out);
+    return out;
+}
+
+// renderBatch([{name, view: ArrayBuffer(176), image: Uint8Array(W*H*4)}, ...]) -- many views and
+// scenes in one launch
+napi_value render_batch(napi_env env, napi_callback_info info) {
+    size_t argc = 1;
+    napi_value argv[1];
+    Native* n = unwrap(env, info, &argc, argv);
+    uint32_t count = 0;
+    napi_get_array_length(env, argv[0], &count);
+    std::vector<gs_batch_view> views(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        napi_value item, vname, vview, vimage;
+        napi_get_element(env, argv[0], i, &item);
+        napi_get_named_property(env, item, "name", &vname);
+        napi_get_named_property(env, item, "view", &vview);
+        napi_get_named_property(env, item, "image", &vimage);
+        char name[256];
+        size_t len = 0;
+        napi_get_value_string_utf8(env, vname, name, sizeof(name), &len);
+        auto it = n->scenes.find(name);
+        if (it == n->scenes.end()) {
+            napi_throw_error(env, nullptr, (std::string("Invalid Gs buffer for name \"") + name + "\"").c_str());
+            return nullptr;
+        }
+        const gs_view* view = view_block(env, vview);
+        if (!view) return nullptr;
+        napi_typedarray_type type;
+        size_t length = 0;
+        void* pixels = nullptr;
+        napi_get_typedarray_info(env, vimage, &type, &length, &pixels, nullptr, nullptr);
+        if (type != napi_uint8_array || length != (size_t)view->texture_size[0] * view->texture_size[1] * 4) {
+            napi_throw_type_error(env, nullptr, "image must be a Uint8Array of W*H*4 bytes");
+            return nullptr;
+        }
+        views[i].scene = it->second;
+        views[i].view = *view;
+        views[i].out = gs_image{GS_MEM_HOST, static_cast<uint8_t*>(pixels), nullptr, nullptr, nullptr};
+    }
+    const int rc = gs_forward_batch(n->ctx, views.data(), count);
+    if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return throw_status(env, rc, n->ctx);
     return nullptr;
 }
 
@@ -166,9 +308,14 @@ napi_value init(napi_env env, napi_value exports) {
         {"setGs", nullptr, set_gs, nullptr, nullptr, nullptr, napi_default, nullptr},
         {"render", nullptr, render, nullptr, nullptr, nullptr, napi_default, nullptr},
         {"timings", nullptr, timings, nullptr, nullptr, nullptr, napi_default, nullptr},
+        {"renderRgb", nullptr, render_rgb, nullptr, nullptr, nullptr, napi_default, nullptr},
+        {"backward", nullptr, backward, nullptr, nullptr, nullptr, napi_default, nullptr},
+        {"loss", nullptr, loss, nullptr, nullptr, nullptr, napi_default, nullptr},
+        {"renderBatch", nullptr, render_batch, nullptr, nullptr, nullptr, napi_default, nullptr},
     };
     napi_value cls;
-    napi_define_class(env, "Native", NAPI_AUTO_LENGTH, construct, nullptr, 4, methods, &cls);
+    napi_define_class(env, "Native", NAPI_AUTO_LENGTH, construct, nullptr, sizeof(methods) / sizeof(methods[0]),
+                      methods, &cls);
     napi_set_named_property(env, exports, "Native", cls);
     return exports;
 }
