@@ -508,7 +508,7 @@ def batched_forward(steps, warmup, local_rank) -> dict:
                     ctx.forward_device(scs[si], views[k], rgba8=imgs[k].data_ptr())
                 per_view.append({"scene": W.BATCH_SCENES[si].count, "res": f"{c.width}x{c.height}",
                                  "ms": round(_timed(stream, one, max(5, steps // 2), warmup), 4)})
-        res[label] = {"config": cfg or {"tile_size": 16, "digit_bits": 8, "raster_batch": 256},
+        res[label] = {"config": cfg or {"tile_size": 16, "digit_bits": 8, "raster_batch": 256, "sort_block": 4096},
                       "plain_ms_per_view": round(ms_plain / len(cams), 4),
                       "batched_ms_per_view": round(ms_batch / len(cams), 4),
                       "plain_Mpix_s": round(pix / ms_plain / 1e3, 1), "batched_Mpix_s": round(pix / ms_batch / 1e3, 1),

@@ -61,6 +61,8 @@ typedef struct gs_config {
     uint32_t max_instance_factor; /* instance budget per Gaussian (MAX_INSTANCE_FACTOR = 64) */
     uint32_t flags;               /* GS_FLAG_* */
     int32_t device;               /* CUDA device ordinal */
+    uint32_t sort_block;          /* keys per radix-sort block (partition): 4096 (default) or 2048; the
+                                     reference sorts in blocks of 256 (radix_parallel.wgsl:20-22) */
 } gs_config;
 
 /* Frame outputs. Any pointer may be NULL. All non-NULL pointers live in `location`. */
@@ -174,8 +176,9 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
 
 /* Autotuner (no counterpart in the reference, whose constants are fixed): times gs_forward_batch of
  * `views` over one scene for every tile size {8,16,32} x radix digit width {4,8} x raster batch
- * depth {32,64,128,256}, `iters` frames each, and returns the fastest configuration (other fields
- * from `base`) and its ms per batch. Creates and destroys its own contexts. */
+ * depth {32,64,128,256} x sort block {2048,4096}, `iters` frames each, and returns the fastest
+ * configuration (other fields from `base`) and its ms per batch. Creates and destroys its own
+ * contexts. */
 int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
                 uint32_t iters, gs_config* best, float* best_ms);
 

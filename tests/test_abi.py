@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_sizes_match_header():
     assert C.sizeof(_abi.View) == 176
-    assert C.sizeof(_abi.Config) == 24
+    assert C.sizeof(_abi.Config) == 28
     assert C.sizeof(_abi.FrameInfo) == 4 * 9
     assert C.sizeof(_abi.Timing) == 28
 
@@ -37,6 +37,7 @@ def test_config_defaults_are_reference_constants():
     cfg = _abi.Config()
     webgs.library().gs_config_default(C.byref(cfg))
     assert (cfg.tile_size, cfg.digit_bits, cfg.raster_batch, cfg.max_instance_factor) == (16, 8, 256, 64)
+    assert cfg.sort_block == 4096
 
 
 def test_version_string():

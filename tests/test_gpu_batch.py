@@ -65,4 +65,6 @@ def test_autotune_picks_a_valid_configuration():
     views = [W.CameraSpec((0.0, 0.0, -4.0), (0, 0, 0), 60.0, 320, 240).view()]
     cfg, ms = webgs.autotune(spec.build(), spec.count, views, iters=2)
     assert cfg["tile_size"] in (8, 16, 32) and cfg["digit_bits"] in (4, 8)
-    assert cfg["raster_batch"] in (32, 64, 128, 256) and ms > 0
+    assert cfg["raster_batch"] in (32, 64, 128, 256) and cfg["sort_block"] in (2048, 4096) and ms > 0
+    with webgs.Context(**cfg) as ctx:  # the pick is a configuration a context accepts
+        assert ctx.config.sort_block == cfg["sort_block"]

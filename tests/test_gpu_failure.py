@@ -50,3 +50,5 @@ def test_invalid_arguments_are_reported_not_thrown(gpu_ctx):
         sc.close()
     with pytest.raises(webgs.GsError):
         webgs.Context(tile_size=12)
+    with pytest.raises(webgs.GsError):
+        webgs.Context(sort_block=1000)

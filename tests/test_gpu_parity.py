@@ -64,6 +64,17 @@ def test_tile_and_digit_configs(tile, digit_bits):
     assert_frame_parity(g, o)
 
 
+@pytest.mark.parametrize("digit_bits", [4, 8])
+def test_small_sort_block_parity(digit_bits):
+    """2048-key sort blocks (the autotuner's other block size) across many partitions."""
+    spec = W.SceneSpec(100_000, 12, 1, 16, 8.0)
+    view = W.CameraSpec((0.0, 0.5, -6.0), (0.0, 0.0, 0.0), 60.0, 640, 480).view()
+    with webgs.Context(digit_bits=digit_bits, sort_block=2048) as ctx:
+        g, o = _run(ctx, spec.build(), spec.count, view)
+    assert o["sorted_count"] > 20 * 2048
+    assert_frame_parity(g, o)
+
+
 @pytest.mark.parametrize("batch", [32, 64, 128, 256])
 def test_raster_batch_depths(batch):
     packed = W.SceneSpec(20_000, 4, 0).build()

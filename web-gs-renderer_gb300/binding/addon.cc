@@ -35,7 +35,7 @@ Native* unwrap(napi_env env, napi_callback_info info, size_t* argc, napi_value* 
     return n;
 }
 
-// new Native({tileSize, digitBits, rasterBatch, maxInstanceFactor, profile, differentiable})
+// new Native({tileSize, digitBits, rasterBatch, maxInstanceFactor, sortBlock, profile, differentiable})
 napi_value construct(napi_env env, napi_callback_info info) {
     size_t argc = 1;
     napi_value argv[1], self;
@@ -46,9 +46,10 @@ napi_value construct(napi_env env, napi_callback_info info) {
         napi_value v;
         bool has = false;
         uint32_t u = 0;
-        const char* keys[] = {"tileSize", "digitBits", "rasterBatch", "maxInstanceFactor"};
-        uint32_t* dst[] = {&cfg.tile_size, &cfg.digit_bits, &cfg.raster_batch, &cfg.max_instance_factor};
-        for (int i = 0; i < 4; ++i) {
+        const char* keys[] = {"tileSize", "digitBits", "rasterBatch", "maxInstanceFactor", "sortBlock"};
+        uint32_t* dst[] = {&cfg.tile_size, &cfg.digit_bits, &cfg.raster_batch, &cfg.max_instance_factor,
+                           &cfg.sort_block};
+        for (int i = 0; i < 5; ++i) {
             napi_has_named_property(env, argv[0], keys[i], &has);
             if (has && napi_get_named_property(env, argv[0], keys[i], &v) == napi_ok &&
                 napi_get_value_uint32(env, v, &u) == napi_ok)

@@ -181,7 +181,8 @@ bool valid_config(const gs_config& c) {
     const bool tile_ok = c.tile_size == 8 || c.tile_size == 16 || c.tile_size == 32;
     const bool digit_ok = c.digit_bits == 4 || c.digit_bits == 8;
     const bool batch_ok = c.raster_batch == 32 || c.raster_batch == 64 || c.raster_batch == 128 || c.raster_batch == 256;
-    return tile_ok && digit_ok && batch_ok && c.max_instance_factor >= 1;
+    const bool block_ok = c.sort_block == kSortPartition || c.sort_block == kSortPartitionMin;
+    return tile_ok && digit_ok && batch_ok && block_ok && c.max_instance_factor >= 1;
 }
 
 // Checks a view block and derives the frame's sizes.
@@ -220,7 +221,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
         GS_CK(f.keys[b].reserve(a.max_instance));
         GS_CK(f.vals[b].reserve(a.max_instance));
     }
-    const size_t sort_parts = ((size_t)a.max_instance + kSortPartition - 1) / kSortPartition;
+    const size_t sort_parts = ((size_t)a.max_instance + ctx->cfg.sort_block - 1) / ctx->cfg.sort_block;
     const size_t scan_parts = ((size_t)a.n + 1 + kScanPartition - 1) / kScanPartition;
     const size_t words = std::max(sort_parts * radix, scan_parts);
     if (words > f.flags.cap || !f.flags.p) {
@@ -274,7 +275,8 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     int cur = 0;
     for (uint32_t p = 0; p < a.passes; ++p) {
         launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
-                        0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s);
+                        0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
+                        ctx->cfg.sort_block);
         cur ^= 1;
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
@@ -381,6 +383,7 @@ void gs_config_default(gs_config* cfg) {
     cfg->max_instance_factor = 64;  // MAX_INSTANCE_FACTOR, renderer.js:16
     cfg->flags = 0;
     cfg->device = 0;
+    cfg->sort_block = 4096;         // keys per sort partition (the reference sorts 256-key blocks)
 }
 
 int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
@@ -935,15 +938,18 @@ int gs_autotune(const gs_config* base, const float* packed, uint32_t count, cons
     const uint32_t tiles[] = {8, 16, 32};
     const uint32_t digits[] = {4, 8};
     const uint32_t batches[] = {32, 64, 128, 256};
+    const uint32_t blocks[] = {kSortPartitionMin, kSortPartition};
     float best_t = 3.0e38f;
     gs_config best_c = b;
     for (uint32_t t : tiles)
         for (uint32_t d : digits)
-            for (uint32_t r : batches) {
+            for (uint32_t r : batches)
+            for (uint32_t sb : blocks) {
                 gs_config c = b;
                 c.tile_size = t;
                 c.digit_bits = d;
                 c.raster_batch = r;
+                c.sort_block = sb;
                 c.flags &= ~(GS_FLAG_PROFILE | GS_FLAG_DIFFERENTIABLE);
                 gs_ctx* ctx = nullptr;
                 if (gs_ctx_create(&c, &ctx) != GS_OK) return GS_ERR_CUDA;
@@ -1005,7 +1011,7 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
     uint32_t* v0 = k0 + n;
     uint32_t* k1 = v0 + n;
     uint32_t* v1 = k1 + n;
-    const size_t words = ((size_t)n + kSortPartition - 1) / kSortPartition * radix;
+    const size_t words = ((size_t)n + ctx->cfg.sort_block - 1) / ctx->cfg.sort_block * radix;
     if (words > ctx->aux_flags.cap || !ctx->aux_flags.p) {
         GS_CK(ctx->aux_flags.reserve(words));
         GS_CK(cudaMemsetAsync(ctx->aux_flags.p, 0, ctx->aux_flags.cap * 8, ctx->stream));
@@ -1023,7 +1029,7 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
         const uint32_t left = key_bits - p * bits;
         const uint32_t dmask = left >= bits ? radix - 1u : (1u << left) - 1u;
         launch_onesweep(bits, kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], nullptr, n, n, p * bits, dmask,
-                        ctl->hist + p * radix, ctl, ctx->aux_flags.p, 1 + p, 0, ctx->stream);
+                        ctl->hist + p * radix, ctl, ctx->aux_flags.p, 1 + p, 0, ctx->stream, ctx->cfg.sort_block);
         cur ^= 1;
     }
     GS_CK(cudaGetLastError());

@@ -284,8 +284,9 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 
 // ---- onesweep radix pass ------------------------------------------------------------------------
 // One stable counting-sort pass on digit (key >> shift) & (RADIX-1) (radix_parallel.wgsl:26-160 in
-// one kernel). Persistent CTAs take partitions of 4096 keys by ticket. Per partition:
-//   - keys load warp-striped (item k of lane l of warp w is element w*512 + k*32 + l), so every
+// one kernel). Persistent CTAs take partitions of 256 x ITEMS keys (4096 or 2048) by ticket. Per
+// partition:
+//   - keys load warp-striped (item k of lane l of warp w is element w*32*ITEMS + k*32 + l), so every
 //     load is a 128-byte line and the warp processes its elements in index order;
 //   - __match_any_sync groups the lanes holding the same digit; a lane's rank is the count of
 //     equal digits in earlier items of its warp plus its rank among the equal lanes (stable);
@@ -294,7 +295,7 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 //     by decoupled lookback (one thread per digit);
 //   - keys/values are staged in shared memory in local sorted order and written out at
 //     global_digit_base + rank, which keeps runs of equal digits contiguous in global memory.
-template <int BITS>
+template <int BITS, int ITEMS>
 __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __restrict__ keys_in,
                                                            const uint32_t* __restrict__ vals_in,
                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
@@ -304,9 +305,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     constexpr uint32_t RADIX = 1u << BITS;
     const uint32_t MASK = dmask & (RADIX - 1u);  // digit mask of this pass (narrower on a last partial digit)
     constexpr uint32_t WARPS = kSortThreads / 32;
-    constexpr uint32_t PER_WARP = kSortItems * 32;
-    __shared__ uint32_t s_keys[kSortPartition];
-    __shared__ uint32_t s_vals[kSortPartition];
+    constexpr uint32_t PER_WARP = ITEMS * 32;
+    constexpr uint32_t PART = kSortThreads * ITEMS;  // keys per partition
+    __shared__ uint32_t s_keys[PART];
+    __shared__ uint32_t s_vals[PART];
     __shared__ uint32_t s_whist[WARPS][RADIX];
     __shared__ uint32_t s_gbase[RADIX];     // global exclusive digit base of this pass
     __shared__ uint32_t s_dstart[RADIX];    // local sorted start of each digit
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
 
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t n = n_dev ? *n_dev : n_host;
-    const uint32_t nparts = (n + kSortPartition - 1u) / kSortPartition;
+    const uint32_t nparts = (n + PART - 1u) / PART;
 
     if (tid == 0) s_seq = ctl->seq + slot;
     bool have_bases = false;
@@ -335,22 +337,22 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             if (tid < RADIX) s_gbase[tid] = ex;
             have_bases = true;
         }
-        const uint32_t base = part * kSortPartition;
-        const uint32_t valid_n = min(kSortPartition, n - base);
+        const uint32_t base = part * PART;
+        const uint32_t valid_n = min(PART, n - base);
 
         for (uint32_t d = lane; d < RADIX; d += 32) s_whist[warp][d] = 0u;
         __syncwarp();
 
-        uint32_t key[kSortItems];
-        uint16_t rank[kSortItems];
+        uint32_t key[ITEMS];
+        uint16_t rank[ITEMS];
         const uint32_t wbase = base + warp * PER_WARP;
 #pragma unroll
-        for (uint32_t k = 0; k < kSortItems; ++k) {
+        for (uint32_t k = 0; k < ITEMS; ++k) {
             const uint32_t idx = wbase + k * 32u + lane;
             key[k] = idx < n ? keys_in[idx] : 0xFFFFFFFFu;
         }
 #pragma unroll
-        for (uint32_t k = 0; k < kSortItems; ++k) {
+        for (uint32_t k = 0; k < ITEMS; ++k) {
             const uint32_t idx = wbase + k * 32u + lane;
             const bool ok = idx < n;
             const uint32_t d = ok ? ((key[k] >> shift) & MASK) : RADIX;  // RADIX marks padding
@@ -425,7 +427,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
         // local sorted order in shared memory; values are read only now, straight into their slot,
         // which keeps them out of registers during the ranking
 #pragma unroll
-        for (uint32_t k = 0; k < kSortItems; ++k) {
+        for (uint32_t k = 0; k < ITEMS; ++k) {
             const uint32_t idx = wbase + k * 32u + lane;
             if (idx < n) {
                 const uint32_t d = (key[k] >> shift) & MASK;
@@ -523,25 +525,32 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
 }
 
 void configure_sort_kernels() {
-    // the largest shared-memory carveout lets more onesweep CTAs (41 KB each) share an SM
-    cudaFuncSetAttribute(k_onesweep<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_onesweep<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    // the largest shared-memory carveout lets more onesweep CTAs (up to 44 KB each) share an SM
+    cudaFuncSetAttribute(k_onesweep<4, 8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<4, 16>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 16>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s) {
-    uint32_t parts = (max_n + kSortPartition - 1u) / kSortPartition;
+                     int grid_cap, cudaStream_t s, uint32_t block) {
+    const bool small = block == kSortPartitionMin;
+    const uint32_t part = small ? kSortPartitionMin : kSortPartition;
+    uint32_t parts = (max_n + part - 1u) / part;
     const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
     if (parts > cap) parts = cap;
     if (parts == 0) parts = 1;
-    if (digit_bits == 4)
-        k_onesweep<4><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, dmask,
-                                                     hist, ctl, flags, slot);
-    else
-        k_onesweep<8><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, dmask,
-                                                     hist, ctl, flags, slot);
+#define GS_ONESWEEP(B, I)                                                                                      \
+    k_onesweep<B, I><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, \
+                                                    dmask, hist, ctl, flags, slot)
+    if (digit_bits == 4) {
+        if (small) GS_ONESWEEP(4, 8); else GS_ONESWEEP(4, 16);
+    } else {
+        if (small) GS_ONESWEEP(8, 8); else GS_ONESWEEP(8, 16);
+    }
+#undef GS_ONESWEEP
 }
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,

@@ -35,14 +35,15 @@ void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uin
 
 // Onesweep LSD radix pass. n comes from *n_dev when non-null, else n_host.
 constexpr uint32_t kSortThreads = 256;
-constexpr uint32_t kSortItems = 16;
-constexpr uint32_t kSortPartition = kSortThreads * kSortItems;
+constexpr uint32_t kSortItems = 16;                            // keys per thread of the largest block
+constexpr uint32_t kSortPartition = kSortThreads * kSortItems; // largest sort block (4096 keys)
+constexpr uint32_t kSortPartitionMin = kSortThreads * 8;       // smallest sort block (2048 keys)
 // Per-device kernel attributes (shared-memory carveout of the sort); call once per context.
 void configure_sort_kernels();
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s);
+                     int grid_cap, cudaStream_t s, uint32_t block = kSortPartition);
 // Digit histograms of all passes over the low key_bits bits, for a standalone sort.
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);

@@ -125,11 +125,12 @@ class Context:
     """One CUDA stream and its frame buffers (include/gs.h gs_ctx)."""
 
     def __init__(self, tile_size: int = 16, digit_bits: int = 8, raster_batch: int = 256,
-                 max_instance_factor: int = 64, flags: int = 0, device: int = 0):
+                 max_instance_factor: int = 64, flags: int = 0, device: int = 0, sort_block: int = 4096):
         lib = library()
         cfg = Config()
         lib.gs_config_default(C.byref(cfg))
         cfg.tile_size, cfg.digit_bits, cfg.raster_batch = tile_size, digit_bits, raster_batch
+        cfg.sort_block = sort_block
         cfg.max_instance_factor, cfg.flags, cfg.device = max_instance_factor, flags, device
         self.config = cfg
         h = C.c_void_p()
@@ -312,8 +313,8 @@ Context.forward_device = _forward_tracking(Context.forward_device)
 
 def autotune(packed: np.ndarray, count: int, views: list, iters: int = 5, device: int = 0,
              max_instance_factor: int = 64) -> tuple[dict, float]:
-    """Sweeps tile size x radix digit width x raster batch depth for a batch of views of one scene
-    (gs_autotune); returns the fastest configuration and its ms per batch."""
+    """Sweeps tile size x radix digit width x raster batch depth x sort block for a batch of views of
+    one scene (gs_autotune); returns the fastest configuration and its ms per batch."""
     base = Config()
     library().gs_config_default(C.byref(base))
     base.device, base.max_instance_factor = device, max_instance_factor
@@ -322,7 +323,8 @@ def autotune(packed: np.ndarray, count: int, views: list, iters: int = 5, device
     p = np.ascontiguousarray(packed, dtype=np.float32)
     _check(library().gs_autotune(C.byref(base), _ptr(p), count, arr, len(views), iters, C.byref(best), C.byref(ms)),
            None, "gs_autotune")
-    return {"tile_size": best.tile_size, "digit_bits": best.digit_bits, "raster_batch": best.raster_batch}, ms.value
+    return {"tile_size": best.tile_size, "digit_bits": best.digit_bits, "raster_batch": best.raster_batch,
+            "sort_block": best.sort_block}, ms.value
 
 
 # ---- Camera (src/renderer/camera.js) -------------------------------------------------------------

@@ -47,6 +47,7 @@ class Config(C.Structure):
     _fields_ = [
         ("tile_size", C.c_uint32), ("digit_bits", C.c_uint32), ("raster_batch", C.c_uint32),
         ("max_instance_factor", C.c_uint32), ("flags", C.c_uint32), ("device", C.c_int32),
+        ("sort_block", C.c_uint32),
     ]
 
 
