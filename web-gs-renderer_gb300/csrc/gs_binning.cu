@@ -17,6 +17,27 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
 // Block-wide exclusive scan of one value per thread (THREADS a multiple of 32). Returns the
 // exclusive prefix; *total receives the block sum. Uses `warp_sums` (THREADS/32 words).
+// Exclusive max-scan over the block (identity 0); warp_sums holds THREADS / 32 + 1 words.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_max(uint32_t v, uint32_t* warp_sums) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl = max(incl, t);
+    }
+    uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = 0u;
+    __syncthreads();
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t prior = 0u;
+    for (uint32_t w = 0; w < warp; ++w) prior = max(prior, warp_sums[w]);
+    __syncthreads();
+    return max(prior, excl);
+}
+
 template <int THREADS>
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
@@ -68,9 +89,9 @@ __global__ void k_frame_begin(FrameCtl* ctl) {
 // 3. offsets[g] are written (offsets[n] = I), the partition holding entry n publishes I and
 //    min(I, max_instance) to FrameCtl (indirect_arg.wgsl:14-27);
 // 4. the partition's instances [excl, excl + total) are emitted by all 256 threads in slot order,
-//    each slot finding its Gaussian by binary search over the partition's local offsets, so one
-//    large splat never serialises a warp; keys are ((ty*tilesPerRow + tx) << 16) | depth16 in
-//    row-major tile order (emit.wgsl:55-66) and slots >= max_instance are dropped (:57-59);
+//    each slot finding its Gaussian in an owner map built per chunk of slots, so one large splat
+//    never serialises a warp; keys are ((ty*tilesPerRow + tx) << 16) | depth16 in row-major tile
+//    order (emit.wgsl:55-66) and slots >= max_instance are dropped (:57-59);
 // 5. the digit histograms of every sort pass are accumulated on the fly (per Gaussian for the
 //    depth digits, per instance for the tile digits).
 __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __restrict__ counts,
@@ -81,8 +102,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
                                                             uint32_t* __restrict__ vals, FrameCtl* ctl,
                                                             uint64_t* flags, uint32_t slot) {
     __shared__ uint32_t s_off[kScanPartition + 1];
-    __shared__ uint2 s_meta[kScanPartition];  // (min, max) packed rects
-    __shared__ uint32_t s_depth[kScanPartition];
+    __shared__ uint2 s_meta[kScanPartition];  // (minX | minY << 16, rect width | depth16 << 16)
+    __shared__ uint32_t s_own[kScanPartition];  // owner (local Gaussian) of each slot of an emit chunk
     __shared__ uint32_t s_hist[8 * 256];
     __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
     __shared__ uint32_t s_part, s_excl, s_seq;
@@ -130,8 +151,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
             s_off[lg] = run;
             if (c[k] != 0u) {
                 const uint4 m = meta[g0 + k];
-                s_meta[lg] = make_uint2(m.x, m.y);
-                s_depth[lg] = m.z & 0xFFFFu;
+                const uint32_t width = (m.y & 0xFFFFu) - (m.x & 0xFFFFu) + 1u;
+                s_meta[lg] = make_uint2(m.x, width | (m.z << 16u));
             }
             run += c[k];
         }
@@ -190,31 +211,62 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
         const uint32_t first = excl + s_off[lg];
         const uint32_t kept = first >= max_instance ? 0u : min(c[k], max_instance - first);
         if (kept == 0u) continue;
-        const uint32_t d16 = s_depth[lg];
+        const uint32_t d16 = s_meta[lg].y >> 16u;
         for (uint32_t p = 0; p < depth_passes; ++p)
             atomicAdd(&s_hist[p * radix + ((d16 >> (p * digit_bits)) & mask)], kept);
     }
 
-    // emit
-    for (uint32_t i = tid; i < total; i += kScanThreads) {
-        const uint32_t slot_i = excl + i;
-        if (slot_i >= max_instance) break;
-        // largest lg with s_off[lg] <= i (counts of that Gaussian > 0 since s_off[lg+1] > i)
-        uint32_t lo = 0, hi = kScanPartition;  // invariant: s_off[lo] <= i < s_off[hi]
-        while (hi - lo > 1u) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_off[mid] <= i) lo = mid; else hi = mid;
+    // emit, in chunks of kScanPartition slots: the owner of every slot of a chunk comes from an owner
+    // map (each Gaussian marks the slot where its run starts, or slot 0 if its run covers the chunk's
+    // start; an inclusive max-scan fills the rest, local indices growing with their offsets), so no
+    // slot searches; the tile of instance k of a w-wide rect is (k / w, k % w) through a float
+    // reciprocal corrected to the exact quotient
+    const uint32_t kept_total = excl >= max_instance ? 0u : min(total, max_instance - excl);
+    for (uint32_t c0 = 0; c0 < kept_total; c0 += kScanPartition) {
+        const uint32_t c1 = c0 + kScanPartition;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) s_own[tid * kScanItems + k] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t lg = tid * kScanItems + k;
+            if (c[k] == 0u) continue;
+            const uint32_t start = s_off[lg];
+            if (start >= c0 && start < c1) s_own[start - c0] = lg;
+            else if (start < c0 && start + c[k] > c0) s_own[0] = lg;
         }
-        const uint32_t k = i - s_off[lo];
-        const uint2 m = s_meta[lo];
-        const uint32_t minX = m.x & 0xFFFFu, minY = m.x >> 16u, maxX = m.y & 0xFFFFu;
-        const uint32_t w = maxX - minX + 1u;
-        const uint32_t ty = minY + k / w, tx = minX + k % w;
-        const uint32_t key = ((ty * tiles_x + tx) << 16u) | s_depth[lo];
-        keys[slot_i] = key;
-        vals[slot_i] = base + lo;
-        for (uint32_t p = depth_passes; p < passes; ++p)
-            atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+        __syncthreads();
+        uint32_t run = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) run = max(run, s_own[tid * kScanItems + k]);
+        const uint32_t before = block_exclusive_max<kScanThreads>(run, s_warp);
+        run = before;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            run = max(run, s_own[tid * kScanItems + k]);
+            s_own[tid * kScanItems + k] = run;
+        }
+        __syncthreads();
+        const uint32_t cn = min(kept_total - c0, kScanPartition);
+        for (uint32_t j = tid; j < cn; j += kScanThreads) {
+            const uint32_t i = c0 + j;
+            const uint32_t lg = s_own[j];
+            const uint32_t k = i - s_off[lg];
+            const uint2 m = s_meta[lg];
+            const uint32_t w = m.y & 0xFFFFu;
+            // k < 2^24 and w < 2^16 are exact floats; the rounded quotient is off by at most one
+            uint32_t q = (uint32_t)__fdividef((float)k, (float)w);
+            int32_t r = (int32_t)(k - q * w);
+            if (r < 0) { --q; r += (int32_t)w; }
+            else if (r >= (int32_t)w) { ++q; r -= (int32_t)w; }
+            const uint32_t ty = (m.x >> 16u) + q, tx = (m.x & 0xFFFFu) + (uint32_t)r;
+            const uint32_t key = ((ty * tiles_x + tx) << 16u) | (m.y >> 16u);
+            keys[excl + i] = key;
+            vals[excl + i] = base + lg;
+            for (uint32_t p = depth_passes; p < passes; ++p)
+                atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
+        }
+        __syncthreads();
     }
     __syncthreads();
     for (uint32_t i = tid; i < passes * radix; i += kScanThreads)
