@@ -2,7 +2,7 @@
 // layout conversions.
 //
 // One thread per Gaussian over the structure-of-arrays scene rows. Each CTA stages its 128-Gaussian
-// slice of the 59 rows in shared memory with bulk copies (TMA, one mbarrier), so the whole 30 KB is
+// slice of the 59 rows in shared memory with bulk copies (TMA, two mbarriers), so the whole 30 KB is
 // in flight before any arithmetic starts and the kernel streams the scene at HBM rate. The
 // arithmetic follows the WGSL source order with no contraction (the file is built with -fmad=false)
 // so that every output bit equals the reference restatement.
@@ -38,36 +38,49 @@ __device__ __forceinline__ M3 tr33(const M3& a) {
 constexpr uint32_t kPreGroup = 128;  // Gaussians (threads) per preprocess CTA
 
 // The CTA's 128-Gaussian slice of all 59 attribute rows is staged in shared memory by bulk copies
-// (cp.async.bulk, 59 x 512 bytes on one mbarrier, issued by one thread), so every CTA has its whole
-// 30 KB in flight at once; threads then read their attributes from shared memory.
+// (cp.async.bulk, 59 x 512 bytes issued by one thread), so every CTA has its whole 30 KB in flight
+// at once; threads then read their attributes from shared memory. The 14 geometry rows (position,
+// log-scale, rotation, f_dc, opacity) complete on one mbarrier and the 45 f_rest rows on another,
+// so the projection and covariance work overlaps the arrival of the SH coefficients.
+
+// Bounded wait on a bulk-copy barrier: on expiry the timeout is recorded and the kernel goes on
+// with what has arrived.
+__device__ __forceinline__ void wait_staged(uint64_t* bar, FrameCtl* ctl) {
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, 0)) {
+        if (++spins > kSpinLimit) {
+            if (threadIdx.x == 0) atomicOr(&ctl->status, kDevTimeout);
+            break;
+        }
+    }
+}
 __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
                                                           const ViewBlock* __restrict__ vb, uint32_t tile,
                                                           float4* __restrict__ rec, uint4* __restrict__ meta,
                                                           uint32_t* __restrict__ counts, FrameCtl* ctl) {
     __shared__ __align__(128) float s_rows[kRows][kPreGroup];
-    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
     __shared__ ViewBlock sv;
     const uint32_t lt = threadIdx.x;
     const uint32_t g0 = blockIdx.x * kPreGroup;
-    if (lt == 0) mbar_init(&s_bar, 1);
+    if (lt == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
     if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
     __syncthreads();
-    if (lt == 0 && g0 < stride) {
+    const bool staged = g0 < stride;
+    if (lt == 0 && staged) {
         // stride and g0 are multiples of 64: every row slice starts 256-byte aligned and spans a
         // multiple of 256 bytes
         const uint32_t cols = min(kPreGroup, stride - g0);
-        mbar_expect_tx(&s_bar, kRows * cols * 4u);
-        for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+        mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
+        for (int r = 0; r < kRowRest; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
+        mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
+        for (int r = kRowRest; r < kRows; ++r)
+            bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
     }
-    if (g0 < stride) {
-        uint32_t spins = 0;
-        while (!mbar_try_wait(&s_bar, 0)) {
-            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
-                if (lt == 0) atomicOr(&ctl->status, kDevTimeout);
-                break;
-            }
-        }
-    }
+    if (staged) wait_staged(&s_bar[0], ctl);
     auto attr = [&](int row) { return s_rows[row][lt]; };
     const uint32_t g = g0 + lt;
     if (g == 0) counts[n] = 0u;  // the N+1-th scan entry (cleared by renderer.js:826)
@@ -89,9 +102,11 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
     const bool near_ok = g < n && !(pv[2] >= -kZNearView);
     const int block_near = __syncthreads_count(near_ok);
     if (threadIdx.x == 0 && block_near) atomicAdd(&ctl->near_pass, (uint32_t)block_near);
-    if (g >= n) return;
-    if (!near_ok) {
-        counts[g] = 0u;
+    // a thread leaves only after the f_rest copies have landed: the CTA's shared memory must not be
+    // released while a bulk copy still writes into it
+    if (g >= n || !near_ok) {
+        if (g < n) counts[g] = 0u;
+        if (staged) wait_staged(&s_bar[1], ctl);
         return;
     }
 #pragma unroll
@@ -230,6 +245,7 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
     w[13] = (kShC3_4 * x) * ((4.0f * szz - sxx) - syy);
     w[14] = (kShC3_5 * z) * (sxx - syy);
     w[15] = (kShC3_6 * x) * (sxx - 3.0f * syy);
+    if (staged) wait_staged(&s_bar[1], ctl);
     float col[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
