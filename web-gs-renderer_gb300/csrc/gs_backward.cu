@@ -238,8 +238,9 @@ constexpr uint32_t kBwdPitch = 132;
 // Chain rule of one visible Gaussian from its 2D gradients d2 = dL/d(pixel.xy, conic, opacity, rgb)
 // back to its 59 attributes. R_(row) reads an attribute, W_(row, v) emits its gradient; every W_ of a
 // row comes after the last R_ of that row, so W_ may overwrite the staged attribute in place.
-template <class RF, class WF>
-__device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const float* __restrict__ d2, RF R_, WF W_) {
+template <class RF, class WF, class SF>
+__device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const float* __restrict__ d2, RF R_, WF W_,
+                                                  SF sh_ready) {
     const float gpx = d2[0], gpy = d2[1], gA = d2[2], gB = d2[3], gC = d2[4], go = d2[5];
     const float p[3] = {R_(0), R_(1), R_(2)};
     float pv[4], clip[4];
@@ -338,6 +339,7 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
     Y[13] = kShC3_4 * dx_ * (4 * zz - xx - yy);
     Y[14] = kShC3_5 * dz_ * (xx - yy);
     Y[15] = kShC3_6 * dx_ * (xx - 3 * yy);
+    sh_ready();  // the f_rest rows arrive on their own barrier
     float gcol[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -414,9 +416,10 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
 }
 
 // One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
-// residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of
-// the 59 attribute rows in shared memory with bulk copies on one mbarrier (as the forward preprocess
-// does), so all of its loads are in flight at once.
+// residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of the 59
+// attribute rows in shared memory with bulk copies (as the forward preprocess does): the geometry rows
+// on one mbarrier and the 45 f_rest rows on another, so the geometric part of the chain rule overlaps
+// the arrival of the SH coefficients.
 //   PACKED  the gradients replace the staged attributes in shared memory and the CTA writes its
 //           slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest blocks, the
 //           layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros;
@@ -429,40 +432,55 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
                                                                    const float* __restrict__ grad2d,
                                                                    float* __restrict__ out, uint32_t* status) {
     __shared__ __align__(128) float s_rows[kRows][kBwdPitch];
-    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
     __shared__ ViewBlock sv;
     const uint32_t lt = threadIdx.x;
     const uint32_t g0 = blockIdx.x * kBwdGroup;
     const uint32_t g = g0 + lt;
     const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
     const bool vis = g < n && counts[g] != 0u;
-    if (lt == 0) mbar_init(&s_bar, 1);
+    if (lt == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
     if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
     const int any = __syncthreads_or(vis);
+    // bounded wait: on expiry the timeout is recorded and the kernel goes on with what is there
+    auto wait_bar = [&](uint64_t* bar) {
+        uint32_t spins = 0;
+        while (!mbar_try_wait(bar, 0)) {
+            if (++spins > kSpinLimit) {
+                if (lt == 0 && status) atomicOr(status, kDevTimeout);
+                break;
+            }
+        }
+    };
     if (any) {
         if (lt == 0) {
             // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and
             // spans a multiple of 256 bytes (g0 < n <= stride)
             const uint32_t cols = min(kBwdGroup, stride - g0);
-            mbar_expect_tx(&s_bar, kRows * cols * 4u);
-            for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+            mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
+            for (int r = 0; r < kRowRest; ++r)
+                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
+            mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
+            for (int r = kRowRest; r < kRows; ++r)
+                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
         }
-        uint32_t spins = 0;
-        while (!mbar_try_wait(&s_bar, 0)) {
-            if (++spins > kSpinLimit) {  // bounded: record the timeout and go on with what is there
-                if (lt == 0 && status) atomicOr(status, kDevTimeout);
-                break;
-            }
-        }
+        wait_bar(&s_bar[0]);
         if (vis) {
             auto R_ = [&](int row) { return s_rows[row][lt]; };
             auto W_ = [&](int row, float v) {
                 if (PACKED) s_rows[row][lt] = v;
                 else atomicAdd(out + (size_t)row * stride + g, v);
             };
-            backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_);
-        } else if (PACKED) {
-            for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
+            backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_, [&]() { wait_bar(&s_bar[1]); });
+        } else {
+            // every thread waits for the f_rest copies before it overwrites its column or leaves: no
+            // bulk copy may still write into shared memory that is reused or released
+            wait_bar(&s_bar[1]);
+            if (PACKED)
+                for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
         }
     }
     if (!PACKED) return;
