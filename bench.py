@@ -145,13 +145,13 @@ def peaks() -> tuple[float, str]:
 
 
 # ---- CPU side ------------------------------------------------------------------------------------------
-def cpu_frame_rate(packed, count, view, target_s: float, row_stride: int = 1) -> dict:
+def cpu_frame_rate(packed, count, view, target_s: float, row_stride: int = 1, threads: int | None = None) -> dict:
     import oracle
     import webgs
 
     vb = webgs.view_bytes(view)
     w, h = int(view.texture_size[0]), int(view.texture_size[1])
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     times, frames = [], 0
     t_end = time.perf_counter() + target_s
     while True:
@@ -338,9 +338,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         r = cpu_frame_rate(packed, spec.count, view, target_s=10.0)
+        r1 = cpu_frame_rate(packed, spec.count, view, target_s=0.0, threads=1)  # one frame on one core
         cpu = {"value": round(r["value"], 4), "unit": "Mpix/s", "cores": r["threads"], "kind": "port",
                "sample": f"{r['frames']} whole frames of the same workload, oracle/ C++ OpenMP, "
-                         f"{r['ms_per_frame']:.0f} ms/frame"}
+                         f"{r['ms_per_frame']:.0f} ms/frame",
+               "value_1core": round(r1["value"], 4), "ms_per_frame_1core": round(r1["ms_per_frame"], 1)}
 
     launches_per_frame = 5 + passes  # frame_begin, preprocess, scan+emit, passes x onesweep, ranges, raster
     line = {

@@ -245,6 +245,11 @@ int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, float* pack
 /* Perturbs a packed scene in place: means += N(0, sigma_mean^2), SH (DC and rest) += N(0, sigma_sh^2). */
 int gs_perturb_scene(float* packed, uint32_t count, uint64_t seed, float sigma_mean, float sigma_sh);
 
+/* The present step without a canvas (blit.wgsl / context.js replaced by a file): writes a host rgba8
+ * image (width x height x 4, row 0 at the top, as the raster writes it) as a binary PPM (P6, alpha
+ * dropped) to `path`. GS_ERR_INVALID for bad arguments or a file that cannot be written. */
+int gs_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -374,4 +375,23 @@ extern "C" int gs_perturb_scene(float* packed, uint32_t count, uint64_t seed, fl
             rest[45 * g + a] = (float)((double)rest[45 * g + a] + (double)sigma_sh * normal01(seed, kPerturbSh, 48 * g + 3 + a));
     }
     return GS_OK;
+}
+
+extern "C" int gs_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height) {
+    if (!path || !rgba8 || width == 0 || height == 0) return GS_ERR_INVALID;
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return GS_ERR_INVALID;
+    bool ok = std::fprintf(f, "P6\n%u %u\n255\n", width, height) > 0;
+    std::vector<uint8_t> row((size_t)width * 3);
+    for (uint32_t y = 0; ok && y < height; ++y) {
+        const uint8_t* src = rgba8 + (size_t)y * width * 4;
+        for (uint32_t x = 0; x < width; ++x) {
+            row[3 * x + 0] = src[4 * x + 0];
+            row[3 * x + 1] = src[4 * x + 1];
+            row[3 * x + 2] = src[4 * x + 2];
+        }
+        ok = std::fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? GS_OK : GS_ERR_INVALID;
 }

@@ -98,6 +98,37 @@ def load_ply(source) -> dict:
     return {"count": n.value, "packed": packed}
 
 
+def save_ppm(path, rgba8: np.ndarray) -> None:
+    """Writes an H x W x 4 rgba8 frame as a binary PPM (gs_write_ppm): the present step of the
+    reference (blit.wgsl to the canvas) as a file."""
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    if img.ndim != 3 or img.shape[2] != 4:
+        raise ValueError("rgba8 must be H x W x 4")
+    _check(library().gs_write_ppm(str(path).encode(), _ptr(img), img.shape[1], img.shape[0]), None,
+           f"gs_write_ppm: cannot write {path}")
+
+
+def save_png(path, rgba8: np.ndarray) -> None:
+    """Writes an H x W x 4 rgba8 frame as an 8-bit RGBA PNG (zlib from the standard library)."""
+    import struct
+    import zlib
+
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    if img.ndim != 3 or img.shape[2] != 4:
+        raise ValueError("rgba8 must be H x W x 4")
+    h, w = img.shape[:2]
+    raw = np.concatenate([np.zeros((h, 1), np.uint8), img.reshape(h, w * 4)], axis=1).tobytes()
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+
+
 def perturb_scene(packed: np.ndarray, count: int, seed: int, sigma_mean: float, sigma_sh: float) -> np.ndarray:
     out = np.array(packed, dtype=np.float32, copy=True)
     _check(library().gs_perturb_scene(_ptr(out), count, seed, sigma_mean, sigma_sh), None, "gs_perturb_scene")

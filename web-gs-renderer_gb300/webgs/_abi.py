@@ -117,6 +117,7 @@ SIGNATURES = [
                                  C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.POINTER(View)]),
     ("gs_synth_scene", C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]),
     ("gs_perturb_scene", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_float]),
+    ("gs_write_ppm", C.c_int, [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]),
     ("gs_ply_parse", C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
 ]
 
