@@ -62,6 +62,7 @@ struct Frame {
     DevBuf<uint32_t> keys[2], vals[2];
     DevBuf<uint64_t> flags;
     DevBuf<uint32_t> ranges;
+    DevBuf<uint32_t> order;  // tiles by decreasing range length: the raster CTAs' tile order
     DevBuf<uint32_t> rgba8, n_contrib;
     DevBuf<float> rgb, final_t;
     DevBuf<float> grad2d, dl_stage;
@@ -229,6 +230,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
         GS_CK(cudaMemsetAsync(f.flags.p, 0, f.flags.cap * sizeof(uint64_t), ctx->stream));
     }
     GS_CK(f.ranges.reserve((size_t)a.tiles_x * a.tiles_y * 2));
+    GS_CK(f.order.reserve((size_t)a.tiles_x * a.tiles_y));
     const size_t pix = (size_t)a.w * a.h;
     GS_CK(f.rgba8.reserve(pix));
     GS_CK(f.rgb.reserve(pix * 3));
@@ -282,9 +284,10 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     if (profile) cudaEventRecord(ctx->ev[3], s);
     cudaMemsetAsync(f.ranges.p, 0, (size_t)a.tiles_x * a.tiles_y * 2 * sizeof(uint32_t), s);
     launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, a.max_instance, 0, s);
+    launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order.p, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
     launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,
-                  a.tiles_x, a.tiles_y, a.out, s);
+                  a.tiles_x, a.tiles_y, a.out, f.order.p, s);
     if (profile) cudaEventRecord(ctx->ev[5], s);
 }
 
@@ -785,7 +788,7 @@ static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const 
     if (ev) cudaEventRecord(ev[0], s);
     launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[f.sorted_buf].p, f.rec.p,
                            scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
-                           f.grad2d.p, s);
+                           f.grad2d.p, f.order.p, s);
     if (ev) cudaEventRecord(ev[1], s);
     launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p, out,
                                packed, &f.ctl.p->status, s);

@@ -136,7 +136,8 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                                                                      const float* __restrict__ final_t,
                                                                      const uint32_t* __restrict__ n_contrib,
                                                                      const float* __restrict__ dl_drgb,
-                                                                     float* __restrict__ grad2d) {
+                                                                     float* __restrict__ grad2d,
+                                                                     const uint32_t* __restrict__ order) {
     constexpr int WX = TILE / 8;
     constexpr int kThreads = TILE * TILE / 2;
     __shared__ float4 s_a[BATCH];
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
     __shared__ uint32_t s_g[BATCH];
     __shared__ uint32_t s_maxl;
 
-    const uint32_t tile = blockIdx.x;
+    const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 8u * (warp / WX);
@@ -502,14 +503,15 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
 template <int TILE>
 void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
                      const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
-                     const float* final_t, const uint32_t* n_contrib, const float* dl, float* grad2d, cudaStream_t s) {
+                     const float* final_t, const uint32_t* n_contrib, const float* dl, float* grad2d,
+                     const uint32_t* order, cudaStream_t s) {
     const uint32_t grid = tiles_x * tiles_y;
     constexpr int threads = TILE * TILE / 2;
     switch (batch) {
-        case 32: k_raster_backward<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
-        case 64: k_raster_backward<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
-        case 128: k_raster_backward<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
-        default: k_raster_backward<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d); break;
+        case 32: k_raster_backward<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        case 64: k_raster_backward<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        case 128: k_raster_backward<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        default: k_raster_backward<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
     }
 }
 
@@ -518,13 +520,13 @@ void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* val
 void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals,
                             const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
-                            const float* dl_drgb, float* grad2d, cudaStream_t s) {
+                            const float* dl_drgb, float* grad2d, const uint32_t* order, cudaStream_t s) {
     if (tile == 8)
-        launch_bwd_tile<8>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+        launch_bwd_tile<8>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
     else if (tile == 32)
-        launch_bwd_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+        launch_bwd_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
     else
-        launch_bwd_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, s);
+        launch_bwd_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
 }
 
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,

@@ -538,6 +538,71 @@ __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCtl*
     }
 }
 
+// ---- tile order: heaviest tiles first ----------------------------------------------------------------
+// The raster CTAs take their tiles from `order` (CTA i renders tile order[i]); CTAs start roughly in
+// index order, so listing the tiles by decreasing range length keeps the long tiles from forming the
+// tail of the launch. Lengths are binned (four bins per octave, 64 bins, longest first) and placed by
+// a counting sort; the order inside a bin is whatever the atomics give and changes no output, since
+// every tile is rendered exactly once either way.
+__device__ __forceinline__ uint32_t order_bin(uint32_t len) {
+    const uint32_t v = len + 1u;
+    const uint32_t msb = 31u - __clz(v);
+    const uint32_t sub = msb >= 2u ? (v >> (msb - 2u)) & 3u : (v << (2u - msb)) & 3u;
+    const uint32_t b = msb * 4u + sub;
+    return 63u - min(b, 63u);
+}
+
+constexpr uint32_t kOrderPer = 8;  // tiles per thread per round (8192 tiles per round of 1024 threads)
+
+__global__ void __launch_bounds__(1024) k_tile_order(const uint32_t* __restrict__ ranges, uint32_t tiles,
+                                                     uint32_t* __restrict__ order) {
+    __shared__ uint32_t s_bin[64];
+    const uint32_t tid = threadIdx.x;
+    if (tid < 64u) s_bin[tid] = 0u;
+    __syncthreads();
+    const uint32_t per_round = blockDim.x * kOrderPer;
+    // the bins of one round's tiles: all of its loads are issued before any is used
+    auto bins = [&](uint32_t r0, uint32_t b[kOrderPer]) {
+        uint2 r[kOrderPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kOrderPer; ++k) {
+            const uint32_t t = r0 + k * blockDim.x + tid;
+            r[k] = t < tiles ? reinterpret_cast<const uint2*>(ranges)[t] : make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kOrderPer; ++k) b[k] = order_bin(r[k].y > r[k].x ? r[k].y - r[k].x : 0u);
+    };
+    uint32_t b[kOrderPer];
+    for (uint32_t r0 = 0; r0 < tiles; r0 += per_round) {
+        bins(r0, b);
+#pragma unroll
+        for (uint32_t k = 0; k < kOrderPer; ++k)
+            if (r0 + k * blockDim.x + tid < tiles) atomicAdd(&s_bin[b[k]], 1u);
+    }
+    __syncthreads();
+    if (tid < 32u) {  // exclusive scan of the 64 bins, two per lane
+        const uint32_t x = s_bin[2u * tid], y = s_bin[2u * tid + 1u];
+        uint32_t incl = x + y;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (tid >= (uint32_t)o) incl += t;
+        }
+        const uint32_t excl = incl - (x + y);
+        s_bin[2u * tid] = excl;
+        s_bin[2u * tid + 1u] = excl + x;
+    }
+    __syncthreads();
+    for (uint32_t r0 = 0; r0 < tiles; r0 += per_round) {
+        if (r0 != 0u || tiles > per_round) bins(r0, b);  // one round: the bins are still in registers
+#pragma unroll
+        for (uint32_t k = 0; k < kOrderPer; ++k) {
+            const uint32_t t = r0 + k * blockDim.x + tid;
+            if (t < tiles) order[atomicAdd(&s_bin[b[k]], 1u)] = t;
+        }
+    }
+}
+
 int sm_count() {
     static int cached = 0;
     if (cached == 0) {
@@ -603,6 +668,10 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
         if (small) GS_ONESWEEP(8, 8); else GS_ONESWEEP(8, 16);
     }
 #undef GS_ONESWEEP
+}
+
+void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* order, cudaStream_t s) {
+    k_tile_order<<<1, 1024, 0, s>>>(ranges, tiles, order);
 }
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,

@@ -52,6 +52,9 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
                            uint32_t slot, cudaStream_t s, uint32_t grid = 0);
 
+// Tiles by decreasing range length (a permutation of 0..tiles-1) for the raster launches.
+void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* order, cudaStream_t s);
+
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
                         int grid_cap, cudaStream_t s);
 
@@ -61,10 +64,11 @@ struct RasterOut {
     float* final_t;      // W*H or null
     uint32_t* n_contrib; // W*H or null
 };
-// ctl (optional) bounds every range by the sorted count; n bounds the Gaussian indices.
+// ctl (optional) bounds every range by the sorted count; n bounds the Gaussian indices; order
+// (optional) is the tile each CTA renders (launch_tile_order), else CTA i renders tile i.
 void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec,
                    uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x,
-                   uint32_t tiles_y, const RasterOut& out, cudaStream_t s);
+                   uint32_t tiles_y, const RasterOut& out, const uint32_t* order, cudaStream_t s);
 
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
 
@@ -74,7 +78,7 @@ void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
 void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals,
                             const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
-                            const float* dl_drgb, float* grad2d, cudaStream_t s);
+                            const float* dl_drgb, float* grad2d, const uint32_t* order, cudaStream_t s);
 // grad2d -> dL/d(attributes), one thread per Gaussian.
 // packed: store into `out` in the packed input layout (59*n floats, zeros for invisible Gaussians);
 // else: add into 59 rows of `stride` floats with FP32 atomics (several views of one scene).

@@ -17,9 +17,13 @@
 //  * warp cull: when staging a splat, the CTA computes the bounding box of the region of the tile
 //    where power >= c_o can hold (gs_raster_common.cuh gives the bound). Every warp tests its 8x4
 //    pixel block against the 32 boxes of a group in parallel (one box per lane, one ballot) and
-//    walks only the splats whose box meets its block, in range order. A skipped splat would have been rejected by every pixel
-//    of the warp at "power < c_o" (or "power > 0"). Contributor counts are range positions, so
-//    skipping does not change them.
+//    walks only the splats whose box meets its block, in range order. A skipped splat would have
+//    been rejected by every pixel of the warp at "power < c_o" (or "power > 0"). Contributor counts
+//    are range positions, so skipping does not change them.
+//
+// CTA i renders tile order[i]: the tiles listed by decreasing range length, so the longest tiles
+// start first instead of forming the tail of the launch (with tiles in index order the clustered
+// scenes left about a third of the launch time to a few long tiles).
 #include "gs_kernels.h"
 #include "gs_raster_common.cuh"
 
@@ -31,7 +35,8 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
                                                         const uint32_t* __restrict__ vals,
                                                         const float4* __restrict__ rec, uint32_t n,
                                                         const FrameCtl* __restrict__ ctl, uint32_t width,
-                                                        uint32_t height, uint32_t tiles_x, RasterOut out) {
+                                                        uint32_t height, uint32_t tiles_x, RasterOut out,
+                                                        const uint32_t* __restrict__ order) {
     constexpr int THREADS = TILE * TILE;
     constexpr int WX = TILE / 8;  // warps across the tile
     __shared__ float4 s_a[BATCH];    // (x, y, conic.x, conic.y)
@@ -39,7 +44,7 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
     __shared__ float2 s_c[BATCH];    // (b, cut)
     __shared__ float4 s_box[BATCH];  // cull box (x0, x1, y0, y1)
 
-    const uint32_t tile = blockIdx.x;
+    const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bx0 = tx * TILE + 8u * (warp % WX), by0 = ty * TILE + 4u * (warp / WX);
@@ -135,14 +140,14 @@ __global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restri
 template <int TILE>
 void launch_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
                  const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
-                 const RasterOut& out, cudaStream_t s) {
+                 const RasterOut& out, const uint32_t* order, cudaStream_t s) {
     const uint32_t grid = tiles_x * tiles_y;
     constexpr int threads = TILE * TILE;
     switch (batch) {
-        case 32: k_raster<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        case 64: k_raster<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        case 128: k_raster<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
-        default: k_raster<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out); break;
+        case 32: k_raster<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 64: k_raster<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 128: k_raster<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        default: k_raster<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
     }
 }
 
@@ -150,10 +155,10 @@ void launch_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, c
 
 void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec,
                    uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x,
-                   uint32_t tiles_y, const RasterOut& out, cudaStream_t s) {
-    if (tile == 8) launch_tile<8>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, s);
-    else if (tile == 32) launch_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, s);
-    else launch_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, s);
+                   uint32_t tiles_y, const RasterOut& out, const uint32_t* order, cudaStream_t s) {
+    if (tile == 8) launch_tile<8>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s);
+    else if (tile == 32) launch_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s);
+    else launch_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s);
 }
 
 }  // namespace gs
