@@ -41,12 +41,15 @@ def test_batch_equals_single_views(scenes):
     np.testing.assert_array_equal(batch[0]["rgb"].view(np.uint32), o["rgb"].view(np.uint32))
 
 
-def test_batch_backward_is_sum_of_views():
+@pytest.mark.parametrize("views,w,h", [(3, 256, 192), (18, 96, 64)])
+def test_batch_backward_is_sum_of_views(views, w, h):
+    """The batched backward (one preprocess backward per group of up to 16 views, the later groups
+    added to the first) equals the sum of the single-view gradients."""
     spec = W.SceneSpec(30_000, 6, 1, 64, 20.0)
     packed = spec.build()
-    cams = [c for _, c in W.orbit_cameras(3, 5, 9.0, fixed_resolution=(256, 192))]
+    cams = [c for _, c in W.orbit_cameras(views, 5, 9.0, fixed_resolution=(w, h))]
     rng = np.random.default_rng(0)
-    dls = [rng.normal(0, 1e-3, (192, 256, 3)).astype(np.float32) for _ in cams]
+    dls = [rng.normal(0, 1e-3, (h, w, 3)).astype(np.float32) for _ in cams]
     with webgs.Context(flags=webgs.GS_FLAG_DIFFERENTIABLE) as ctx:
         sc = ctx.upload(packed, spec.count)
         ctx.forward_batch([(sc, c.view()) for c in cams], rgba8=False, rgb=True)

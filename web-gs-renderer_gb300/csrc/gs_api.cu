@@ -130,7 +130,7 @@ struct gs_ctx {
     DevBuf<uint64_t> aux_flags;
     DevBuf<uint32_t> aux_u32;
     DevBuf<float> aux_f32;
-    DevBuf<float> grows, grad_stage, loss_scratch, loss_io;
+    DevBuf<float> grad_stage, loss_scratch, loss_io;
     DevBuf<double> loss_sums;
     FrameCtl* h_aux = nullptr;
 
@@ -403,6 +403,7 @@ int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
     }
     if (cudaSetDevice(c.device) != cudaSuccess) return GS_ERR_CUDA;
     configure_sort_kernels();
+    configure_backward_kernels();
     gs_ctx* ctx = new gs_ctx();
     ctx->cfg = c;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -457,7 +458,7 @@ int gs_ctx_destroy(gs_ctx* ctx) {
         delete f;
     }
     ctx->aux_ctl.release(); ctx->aux_flags.release(); ctx->aux_u32.release(); ctx->aux_f32.release();
-    ctx->grows.release(); ctx->grad_stage.release(); ctx->loss_scratch.release(); ctx->loss_io.release();
+    ctx->grad_stage.release(); ctx->loss_scratch.release(); ctx->loss_io.release();
     ctx->loss_sums.release(); ctx->d_bviews.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -779,10 +780,9 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 }
 
 // ---- backward --------------------------------------------------------------------------------------
-// Raster backward of frame f into f.grad2d, then the preprocess backward: packed, into `out` in the
-// packed layout; else added into the rows of ctx->grows.
-static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, float* out, bool packed,
-                            cudaStream_t s, cudaEvent_t* ev = nullptr) {
+// Raster backward of frame f into f.grad2d (dL/d of its per-Gaussian 2D quantities).
+static int enqueue_raster_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, cudaStream_t s,
+                                   cudaEvent_t* ev = nullptr) {
     GS_CK(f.grad2d.reserve((size_t)scene->n * 9));
     if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
     if (ev) cudaEventRecord(ev[0], s);
@@ -790,25 +790,20 @@ static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const 
                            scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
                            f.grad2d.p, f.order.p, s);
     if (ev) cudaEventRecord(ev[1], s);
-    launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p, out,
-                               packed, &f.ctl.p->status, s);
-    if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
     return GS_OK;
 }
 
-static int finish_grads(gs_ctx* ctx, const gs_scene* scene, float* grad_packed, int32_t location) {
-    const uint32_t n = scene->n;
-    if (location == GS_MEM_DEVICE) {
-        launch_rows_to_pack(ctx->grows.p, n, scene->stride, grad_packed, ctx->stream);
-        GS_CK(cudaGetLastError());
-        return GS_OK;
-    }
-    GS_CK(ctx->grad_stage.reserve((size_t)n * kRows));
-    launch_rows_to_pack(ctx->grows.p, n, scene->stride, ctx->grad_stage.p, ctx->stream);
+// Raster backward of frame f into f.grad2d, then the preprocess backward into `out` in the packed
+// layout.
+static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, float* out, cudaStream_t s,
+                            cudaEvent_t* ev = nullptr) {
+    const int rc = enqueue_raster_backward(ctx, f, scene, dl, s, ev);
+    if (rc != GS_OK) return rc;
+    launch_preprocess_backward(scene->rows, scene->stride, scene->n, f.view_used, f.counts.p, f.grad2d.p, out,
+                               &f.ctl.p->status, s);
+    if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
-    if (n) GS_CK(cudaMemcpyAsync(grad_packed, ctx->grad_stage.p, (size_t)n * kRows * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    GS_CK(cudaStreamSynchronize(ctx->stream));
     return GS_OK;
 }
 
@@ -834,7 +829,7 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
         out = ctx->grad_stage.p;
     }
     const bool profile = (ctx->cfg.flags & GS_FLAG_PROFILE) != 0;
-    const int rc = enqueue_backward(ctx, f, scene, dl, out, true, ctx->stream, profile ? ctx->bev : nullptr);
+    const int rc = enqueue_backward(ctx, f, scene, dl, out, ctx->stream, profile ? ctx->bev : nullptr);
     if (rc != GS_OK) return rc;
     ctx->have_bwd = profile;
     GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -859,8 +854,12 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
             return fail(ctx, GS_ERR_STATE, "gs_backward_batch: view " + std::to_string(i) + " of the last batch is not of this scene");
     }
     GS_CK(cudaSetDevice(ctx->cfg.device));
-    GS_CK(ctx->grows.reserve((size_t)scene->stride * kRows));
-    GS_CK(cudaMemsetAsync(ctx->grows.p, 0, (size_t)scene->stride * kRows * sizeof(float), ctx->stream));
+    const size_t nfloats = (size_t)scene->n * kRows;
+    float* out = grad_packed;
+    if (location == GS_MEM_HOST) {
+        GS_CK(ctx->grad_stage.reserve(nfloats));
+        out = ctx->grad_stage.p;
+    }
     std::vector<const float*> dls(count);
     for (uint32_t i = 0; i < count; ++i) {
         Frame& f = *ctx->batch[i];
@@ -872,24 +871,40 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
             dls[i] = f.dl_stage.p;
         }
     }
-    // views run concurrently on the side streams; their Gaussian gradients meet in grows by atomics
+    // the views' raster backwards run concurrently on the side streams, each into its own frame's 2D
+    // gradients; one preprocess backward per group of up to 16 views then reads the scene once and
+    // sums the views' attribute gradients in the packed layout
     GS_CK(cudaEventRecord(ctx->fork, ctx->stream));
     const int used = (int)std::min<uint32_t>(count, kSideStreams);
     for (int s = 0; s < used; ++s) GS_CK(cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0));
     for (uint32_t i = 0; i < count; ++i) {
-        const int rc = enqueue_backward(ctx, *ctx->batch[i], scene, dls[i], ctx->grows.p, false, ctx->side[i % used]);
+        const int rc = enqueue_raster_backward(ctx, *ctx->batch[i], scene, dls[i], ctx->side[i % used]);
         if (rc != GS_OK) return rc;
     }
     for (int s = 0; s < used; ++s) {
         GS_CK(cudaEventRecord(ctx->join[s], ctx->side[s]));
         GS_CK(cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0));
     }
+    for (uint32_t g0 = 0; g0 < count; g0 += kMaxMultiViews) {
+        MultiViewGrads mv{};
+        mv.count = std::min<uint32_t>(kMaxMultiViews, count - g0);
+        for (uint32_t v = 0; v < mv.count; ++v) {
+            Frame& f = *ctx->batch[g0 + v];
+            mv.view[v] = f.view_used;
+            mv.counts[v] = f.counts.p;
+            mv.grad2d[v] = f.grad2d.p;
+        }
+        launch_preprocess_backward_multi(scene->rows, scene->stride, scene->n, mv, out, g0 != 0,
+                                         &ctx->batch[g0]->ctl.p->status, ctx->stream);
+    }
+    GS_CK(cudaGetLastError());
     for (uint32_t i = 0; i < count; ++i) {
         Frame& f = *ctx->batch[i];
         GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     }
-    const int rc = finish_grads(ctx, scene, grad_packed, location);
-    if (rc != GS_OK || location != GS_MEM_HOST) return rc;
+    if (location == GS_MEM_DEVICE) return GS_OK;
+    if (nfloats) GS_CK(cudaMemcpyAsync(grad_packed, out, nfloats * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
     uint32_t status = 0;
     for (uint32_t i = 0; i < count; ++i) status |= ctx->batch[i]->h_ctl->status;
     return status_to_code(ctx, status & kDevTimeout);  // an overflow was reported by the forward

@@ -1,5 +1,5 @@
 // gs_backward.cu -- gradients of the splat pipeline (no counterpart in the reference, which only
-// renders). Two kernels:
+// renders). Three kernels:
 //   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
 //                         contributor, recomputing power and alpha bit for bit as the forward did
 //                         (same pinned arithmetic, the forward's warp cull box), recovering T by
@@ -8,8 +8,10 @@
 //                         issue the atomics;
 //   k_preprocess_backward one thread per Gaussian: chain rule back through colour (SH), sigmoid,
 //                         conic inverse, 2D covariance J W Sigma W^T J^T, the rotation / scale
-//                         factorisation, and the projection, into the 59 attributes (stored in
-//                         the packed input layout, or added into attribute rows for a batch).
+//                         factorisation, and the projection, into the 59 attributes in the
+//                         packed input layout;
+//   k_preprocess_backward_multi  the same for several views of one scene, reading the scene once
+//                         and summing the views' gradients.
 // Conventions: gradients flow through the fp32 RGB before quantization; culled Gaussians, skipped
 // pairs and splats after a pixel's termination get none; active clamps (alpha 0.99, colour >= 0)
 // pass none; where the frustum guard clamps t.x/t.z (t.y/t.z) no gradient flows through t.x (t.y),
@@ -420,13 +422,9 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
 // residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of the 59
 // attribute rows in shared memory with bulk copies (as the forward preprocess does): the geometry rows
 // on one mbarrier and the 45 f_rest rows on another, so the geometric part of the chain rule overlaps
-// the arrival of the SH coefficients.
-//   PACKED  the gradients replace the staged attributes in shared memory and the CTA writes its
-//           slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest blocks, the
-//           layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros;
-//   !PACKED the gradients are added with FP32 atomics into 59 rows of `stride` floats (several views
-//           of one scene accumulate there; invisible Gaussians add nothing).
-template <bool PACKED>
+// the arrival of the SH coefficients. The gradients replace the staged attributes in shared memory
+// and the CTA writes its slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest
+// blocks, the layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros.
 __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
                                                                    uint32_t n, const ViewBlock* __restrict__ vb,
                                                                    const uint32_t* __restrict__ counts,
@@ -471,20 +469,15 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
         wait_bar(&s_bar[0]);
         if (vis) {
             auto R_ = [&](int row) { return s_rows[row][lt]; };
-            auto W_ = [&](int row, float v) {
-                if (PACKED) s_rows[row][lt] = v;
-                else atomicAdd(out + (size_t)row * stride + g, v);
-            };
+            auto W_ = [&](int row, float v) { s_rows[row][lt] = v; };
             backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_, [&]() { wait_bar(&s_bar[1]); });
         } else {
             // every thread waits for the f_rest copies before it overwrites its column or leaves: no
             // bulk copy may still write into shared memory that is reused or released
             wait_bar(&s_bar[1]);
-            if (PACKED)
-                for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
+            for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
         }
     }
-    if (!PACKED) return;
     __syncthreads();
     // the CTA's Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute block
     struct Block { uint32_t row, width, base; };
@@ -497,6 +490,69 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
         const uint32_t total = bk.width * cnt;
         for (uint32_t i = lt; i < total; i += kBwdGroup)
             dst[i] = any ? s_rows[bk.row + i % bk.width][i / bk.width] : 0.0f;
+    }
+}
+
+// Several views of one scene: one thread per Gaussian stages the 59 attribute rows once (bulk copies)
+// and runs the chain rule for every view that sees the Gaussian, summing the views' gradients in a
+// shared-memory tile of its own column; the CTA then writes its slice of the packed layout with
+// coalesced stores (stored, or added to what an earlier group of views wrote). The scene is read
+// once per batch instead of once per view, and no atomics, clearing or transpose pass are needed.
+__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward_multi(const float* __restrict__ rows,
+                                                                         uint32_t stride, uint32_t n,
+                                                                         MultiViewGrads mv, float* __restrict__ out,
+                                                                         int add, uint32_t* status) {
+    extern __shared__ __align__(128) float s_dyn[];
+    float(*s_rows)[kBwdPitch] = reinterpret_cast<float(*)[kBwdPitch]>(s_dyn);
+    float(*s_grad)[kBwdPitch] = reinterpret_cast<float(*)[kBwdPitch]>(s_dyn + kRows * kBwdPitch);
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ ViewBlock sv;
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kBwdGroup;
+    const uint32_t g = g0 + lt;
+    const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
+    uint32_t seen = 0u;                           // views that see this Gaussian (bit per view)
+    for (uint32_t v = 0; v < mv.count; ++v)
+        if (g < n && mv.counts[v][g] != 0u) seen |= 1u << v;
+    if (lt == 0) mbar_init(&s_bar, 1);
+    for (int r = 0; r < kRows; ++r) s_grad[r][lt] = 0.0f;
+    const int any = __syncthreads_or(seen != 0u);
+    if (any) {
+        if (lt == 0) {
+            // stride and g0 are multiples of 64 floats: 256-byte aligned slices of 256-byte multiples
+            const uint32_t cols = min(kBwdGroup, stride - g0);
+            mbar_expect_tx(&s_bar, kRows * cols * 4u);
+            for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+        }
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0)) {  // every thread waits: no copy may outlive the CTA
+            if (++spins > kSpinLimit) {
+                if (lt == 0 && status) atomicOr(status, kDevTimeout);
+                break;
+            }
+        }
+        auto R_ = [&](int row) { return s_rows[row][lt]; };
+        auto W_ = [&](int row, float val) { s_grad[row][lt] += val; };
+        for (uint32_t v = 0; v < mv.count; ++v) {
+            __syncthreads();  // sv is rewritten per view
+            if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(mv.view[v])[lt];
+            __syncthreads();
+            if (seen & (1u << v)) backward_gaussian(sv, mv.grad2d[v] + (size_t)9 * g, R_, W_, []() {});
+        }
+    }
+    __syncthreads();
+    struct Block { uint32_t row, width, base; };
+    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
+                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
+#pragma unroll
+    for (int bi = 0; bi < 6; ++bi) {
+        const Block bk = blocks[bi];
+        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
+        const uint32_t total = bk.width * cnt;
+        for (uint32_t i = lt; i < total; i += kBwdGroup) {
+            const float val = s_grad[bk.row + i % bk.width][i / bk.width];
+            dst[i] = add ? dst[i] + val : val;
+        }
     }
 }
 
@@ -529,15 +585,26 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
         launch_bwd_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
 }
 
+size_t preprocess_backward_multi_smem() { return (size_t)2 * kRows * kBwdPitch * sizeof(float); }
+
+void configure_backward_kernels() {
+    cudaFuncSetAttribute(k_preprocess_backward_multi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)preprocess_backward_multi_smem());
+}
+
+void launch_preprocess_backward_multi(const float* rows, uint32_t stride, uint32_t n, const MultiViewGrads& mv,
+                                      float* out, bool add, uint32_t* status, cudaStream_t s) {
+    if (n == 0 || mv.count == 0) return;
+    k_preprocess_backward_multi<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, preprocess_backward_multi_smem(), s>>>(
+        rows, stride, n, mv, out, add ? 1 : 0, status);
+}
+
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* out, bool packed,
-                                uint32_t* status, cudaStream_t s) {
+                                const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
+                                cudaStream_t s) {
     if (n == 0) return;
-    const uint32_t grid = (n + kBwdGroup - 1u) / kBwdGroup;
-    if (packed)
-        k_preprocess_backward<true><<<grid, kBwdGroup, 0, s>>>(rows, stride, n, view, counts, grad2d, out, status);
-    else
-        k_preprocess_backward<false><<<grid, kBwdGroup, 0, s>>>(rows, stride, n, view, counts, grad2d, out, status);
+    k_preprocess_backward<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, 0, s>>>(rows, stride, n, view, counts,
+                                                                                grad2d, out, status);
 }
 
 }  // namespace gs

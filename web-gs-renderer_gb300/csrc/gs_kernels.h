@@ -17,7 +17,6 @@ constexpr int kRecFloat4 = 3;
 // packed (reference layout, preprocess.wgsl:16-24) -> rows of the structure-of-arrays layout.
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s);
 // rows -> packed (used for gradients).
-void launch_rows_to_pack(const float* rows, uint32_t n, uint32_t stride, float* packed, cudaStream_t s);
 
 // ---- frame ----------------------------------------------------------------------------------
 void launch_frame_begin(FrameCtl* ctl, cudaStream_t s);
@@ -79,12 +78,25 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
                             const float4* rec, uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height,
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
                             const float* dl_drgb, float* grad2d, const uint32_t* order, cudaStream_t s);
-// grad2d -> dL/d(attributes), one thread per Gaussian.
-// packed: store into `out` in the packed input layout (59*n floats, zeros for invisible Gaussians);
-// else: add into 59 rows of `stride` floats with FP32 atomics (several views of one scene).
+// Up to kMaxMultiViews views of one scene for launch_preprocess_backward_multi.
+constexpr uint32_t kMaxMultiViews = 16;
+struct MultiViewGrads {
+    const ViewBlock* view[kMaxMultiViews];
+    const uint32_t* counts[kMaxMultiViews];
+    const float* grad2d[kMaxMultiViews];
+    uint32_t count;
+};
+// Sum over the views of their dL/d(attributes), written in the packed layout into `out` (add: added
+// to what `out` holds). Call configure_backward_kernels once per device first.
+void configure_backward_kernels();
+void launch_preprocess_backward_multi(const float* rows, uint32_t stride, uint32_t n, const MultiViewGrads& mv,
+                                      float* out, bool add, uint32_t* status, cudaStream_t s);
+
+// grad2d -> dL/d(attributes), one thread per Gaussian, stored into `out` in the packed input layout
+// (59*n floats, zeros for invisible Gaussians).
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* out, bool packed,
-                                uint32_t* status, cudaStream_t s);
+                                const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
+                                cudaStream_t s);
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------
 size_t loss_scratch_floats(uint32_t width, uint32_t height);

@@ -299,7 +299,7 @@ __device__ __forceinline__ void attr_block(uint32_t b, uint32_t& row0, uint32_t&
         default: row0 = 14; width = 45; off = 14; break; // f_rest
     }
 }
-constexpr uint32_t kTransposeGroup = 128;  // Gaussians per CTA of the layout transposes
+constexpr uint32_t kTransposeGroup = 128;  // Gaussians per CTA of the layout transpose
 
 // packed -> rows. A CTA moves kTransposeGroup Gaussians of one attribute block: one coalesced read
 // of the block's contiguous chunk into shared memory, then one coalesced write per row. Padding
@@ -320,23 +320,6 @@ __global__ void __launch_bounds__(256) k_pack_to_rows(const float* __restrict__ 
     }
 }
 
-// rows -> packed, the same tiling in the other direction.
-__global__ void __launch_bounds__(256) k_rows_to_pack(const float* __restrict__ rows, uint32_t n, uint32_t stride,
-                                                      float* __restrict__ packed) {
-    __shared__ float s[kTransposeGroup * 45];
-    uint32_t row0, width, off;
-    attr_block(blockIdx.y, row0, width, off);
-    const uint32_t g0 = blockIdx.x * kTransposeGroup;
-    const uint32_t cnt = min(kTransposeGroup, n - g0);
-    for (uint32_t i = threadIdx.x; i < width * kTransposeGroup; i += blockDim.x) {
-        const uint32_t c = i / kTransposeGroup, lg = i % kTransposeGroup;
-        if (lg < cnt) s[lg * width + c] = rows[(size_t)(row0 + c) * stride + g0 + lg];
-    }
-    __syncthreads();
-    float* dst = packed + (uint64_t)off * n + (uint64_t)g0 * width;
-    for (uint32_t i = threadIdx.x; i < cnt * width; i += blockDim.x) dst[i] = s[i];
-}
-
 __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = pinned_expf(x[i]);
@@ -353,12 +336,6 @@ void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const Vie
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
     dim3 grid((stride + kTransposeGroup - 1u) / kTransposeGroup, 6);
     k_pack_to_rows<<<grid, 256, 0, s>>>(packed, n, stride, rows);
-}
-
-void launch_rows_to_pack(const float* rows, uint32_t n, uint32_t stride, float* packed, cudaStream_t s) {
-    if (n == 0) return;
-    dim3 grid((n + kTransposeGroup - 1u) / kTransposeGroup, 6);
-    k_rows_to_pack<<<grid, 256, 0, s>>>(rows, n, stride, packed);
 }
 
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s) {
