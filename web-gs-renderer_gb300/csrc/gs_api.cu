@@ -262,14 +262,17 @@ RasterOut raster_out(const gs_ctx* ctx, Frame& f, const gs_image* out) {
     return ro;
 }
 
-// Enqueues one frame (renderer.js:822-932) on stream s.
-void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bool profile) {
+// Enqueues one frame (renderer.js:822-932) on stream s; preprocessed: its frame control block was
+// reset and its preprocess done already (by a multi-view preprocess of its scene).
+void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bool profile, bool preprocessed = false) {
     const uint32_t bits = ctx->cfg.digit_bits, radix = 1u << bits;
     FrameCtl* ctl = f.ctl.p;
     if (profile) cudaEventRecord(ctx->ev[0], s);
-    launch_frame_begin(ctl, s);
-    launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p, f.counts.p,
-                      ctl, s);
+    if (!preprocessed) {
+        launch_frame_begin(ctl, s);
+        launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p,
+                          f.counts.p, ctl, s);
+    }
     if (profile) cudaEventRecord(ctx->ev[1], s);
     launch_scan_emit(f.counts.p, f.meta.p, a.n, a.tiles_x, a.max_instance, bits, a.passes, f.offsets.p, f.keys[0].p,
                      f.vals[0].p, ctl, f.flags.p, 0, s);
@@ -333,11 +336,39 @@ int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, con
         if (frames.size() == 1) {
             enqueue_frame(ctx, *frames[0], args[0], ctx->stream, false);
         } else {
+            // views of one scene are preprocessed together (one pass over the scene's attributes per
+            // group of up to 16 views), on the main stream before the fork
+            std::vector<char> pre(frames.size(), 0);
+            for (size_t i = 0; i < frames.size(); ++i) {
+                if (pre[i]) continue;
+                std::vector<size_t> group;
+                for (size_t j = i; j < frames.size(); ++j)
+                    if (!pre[j] && args[j].scene == args[i].scene) group.push_back(j);
+                if (group.size() < 2) continue;
+                for (size_t c0 = 0; c0 < group.size(); c0 += kMaxMultiViews) {
+                    MultiViewFrames mv{};
+                    mv.count = (uint32_t)std::min<size_t>(kMaxMultiViews, group.size() - c0);
+                    for (uint32_t v = 0; v < mv.count; ++v) {
+                        const size_t j = group[c0 + v];
+                        Frame& f = *frames[j];
+                        launch_frame_begin(f.ctl.p, ctx->stream);
+                        mv.view[v] = args[j].view;
+                        mv.rec[v] = f.rec.p;
+                        mv.meta[v] = f.meta.p;
+                        mv.counts[v] = f.counts.p;
+                        mv.ctl[v] = f.ctl.p;
+                        pre[j] = 1;
+                    }
+                    launch_preprocess_multi(args[i].scene->rows, args[i].scene->stride, args[i].n,
+                                            ctx->cfg.tile_size, mv, ctx->stream);
+                }
+            }
             // views are independent: fork them over the side streams so small views fill the GPU together
             cudaEventRecord(ctx->fork, ctx->stream);
             const int used = (int)std::min<size_t>(frames.size(), kSideStreams);
             for (int s = 0; s < used; ++s) cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0);
-            for (size_t i = 0; i < frames.size(); ++i) enqueue_frame(ctx, *frames[i], args[i], ctx->side[i % used], false);
+            for (size_t i = 0; i < frames.size(); ++i)
+                enqueue_frame(ctx, *frames[i], args[i], ctx->side[i % used], false, pre[i] != 0);
             for (int s = 0; s < used; ++s) {
                 cudaEventRecord(ctx->join[s], ctx->side[s]);
                 cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0);

@@ -21,6 +21,21 @@ void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float
 // ---- frame ----------------------------------------------------------------------------------
 void launch_frame_begin(FrameCtl* ctl, cudaStream_t s);
 
+// Up to kMaxMultiViews views of one scene for launch_preprocess_multi: each view's block and frame
+// outputs.
+constexpr uint32_t kMaxMultiViews = 16;
+struct MultiViewFrames {
+    const ViewBlock* view[kMaxMultiViews];
+    float4* rec[kMaxMultiViews];
+    uint4* meta[kMaxMultiViews];
+    uint32_t* counts[kMaxMultiViews];
+    FrameCtl* ctl[kMaxMultiViews];
+    uint32_t count;
+};
+// The preprocess of several views of one scene in one pass over the scene's attribute rows (each
+// view's FrameCtl must have been reset by launch_frame_begin).
+void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uint32_t tile, const MultiViewFrames& mv,
+                             cudaStream_t s);
 void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
                        float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s);
 
@@ -79,7 +94,6 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
                             uint32_t tiles_x, uint32_t tiles_y, const float* final_t, const uint32_t* n_contrib,
                             const float* dl_drgb, float* grad2d, const uint32_t* order, cudaStream_t s);
 // Up to kMaxMultiViews views of one scene for launch_preprocess_backward_multi.
-constexpr uint32_t kMaxMultiViews = 16;
 struct MultiViewGrads {
     const ViewBlock* view[kMaxMultiViews];
     const uint32_t* counts[kMaxMultiViews];

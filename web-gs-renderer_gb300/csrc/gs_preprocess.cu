@@ -54,39 +54,16 @@ __device__ __forceinline__ void wait_staged(uint64_t* bar, FrameCtl* ctl) {
         }
     }
 }
-__global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
-                                                          const ViewBlock* __restrict__ vb, uint32_t tile,
-                                                          float4* __restrict__ rec, uint4* __restrict__ meta,
-                                                          uint32_t* __restrict__ counts, FrameCtl* ctl) {
-    __shared__ __align__(128) float s_rows[kRows][kPreGroup];
-    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
-    __shared__ ViewBlock sv;
-    const uint32_t lt = threadIdx.x;
-    const uint32_t g0 = blockIdx.x * kPreGroup;
-    if (lt == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
-    }
-    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
-    __syncthreads();
-    const bool staged = g0 < stride;
-    if (lt == 0 && staged) {
-        // stride and g0 are multiples of 64: every row slice starts 256-byte aligned and spans a
-        // multiple of 256 bytes
-        const uint32_t cols = min(kPreGroup, stride - g0);
-        mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
-        for (int r = 0; r < kRowRest; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
-        mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
-        for (int r = kRowRest; r < kRows; ++r)
-            bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
-    }
-    if (staged) wait_staged(&s_bar[0], ctl);
-    auto attr = [&](int row) { return s_rows[row][lt]; };
-    const uint32_t g = g0 + lt;
-    if (g == 0) counts[n] = 0u;  // the N+1-th scan entry (cleared by renderer.js:826)
-    const float px = g < n ? attr(kRowPos + 0) : 0.0f;  // out-of-range threads compute on zeros, write nothing
-    const float py = g < n ? attr(kRowPos + 1) : 0.0f;
-    const float pz = g < n ? attr(kRowPos + 2) : 0.0f;
+// One Gaussian g of one view (preprocess.wgsl:58-143): writes its raster record, rect/depth16 and
+// tile count, or a zero count when it is culled. attr(row) reads a staged attribute; sh_ready() is
+// called before the first f_rest read. Returns whether the Gaussian passed the near plane.
+template <class AF, class SF>
+__device__ __forceinline__ bool preprocess_gaussian(uint32_t g, const ViewBlock& sv, uint32_t tile, AF attr,
+                                                    SF sh_ready, float4* __restrict__ rec, uint4* __restrict__ meta,
+                                                    uint32_t* __restrict__ counts) {
+    const float px = attr(kRowPos + 0);
+    const float py = attr(kRowPos + 1);
+    const float pz = attr(kRowPos + 2);
 
     // uniforms.view * vec4f(position, 1.0f)  (:79)
     float pv[4], clip[4];
@@ -98,16 +75,10 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
         s = s + sv.view[3 * 4 + i] * 1.0f;
         pv[i] = s;
     }
-    // near culling (:83); the block counts its survivors for the frame statistics
-    const bool near_ok = g < n && !(pv[2] >= -kZNearView);
-    const int block_near = __syncthreads_count(near_ok);
-    if (threadIdx.x == 0 && block_near) atomicAdd(&ctl->near_pass, (uint32_t)block_near);
-    // a thread leaves only after the f_rest copies have landed: the CTA's shared memory must not be
-    // released while a bulk copy still writes into it
-    if (g >= n || !near_ok) {
-        if (g < n) counts[g] = 0u;
-        if (staged) wait_staged(&s_bar[1], ctl);
-        return;
+    // near culling (:83)
+    if (pv[2] >= -kZNearView) {
+        counts[g] = 0u;
+        return false;
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -245,7 +216,7 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
     w[13] = (kShC3_4 * x) * ((4.0f * szz - sxx) - syy);
     w[14] = (kShC3_5 * z) * (sxx - syy);
     w[15] = (kShC3_6 * x) * (sxx - 3.0f * syy);
-    if (staged) wait_staged(&s_bar[1], ctl);
+    sh_ready();  // the f_rest rows may arrive after the geometry rows
     float col[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -269,7 +240,7 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
     // frustum culling (:117-120)
     if (pixx + radius < 0.0f || pixx - radius > W || pixy + radius < 0.0f || pixy - radius > H) {
         counts[g] = 0u;
-        return;
+        return true;
     }
     // tile AABB, depth16, tilesTouched (:122-143)
     const float bminx = pixx - radius, bminy = pixy - radius;
@@ -285,6 +256,89 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
     const uint32_t depthU16 = (uint32_t)(fminf(fmaxf(ndcz, 0.0f), 1.0f) * 65535.0f);
     counts[g] = (maxTileX - minTileX + 1u) * (maxTileY - minTileY + 1u);
     meta[g] = make_uint4((minTileY << 16u) | minTileX, (maxTileY << 16u) | maxTileX, depthU16, 0u);
+    return true;
+}
+
+__global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restrict__ rows, uint32_t stride, uint32_t n,
+                                                          const ViewBlock* __restrict__ vb, uint32_t tile,
+                                                          float4* __restrict__ rec, uint4* __restrict__ meta,
+                                                          uint32_t* __restrict__ counts, FrameCtl* ctl) {
+    __shared__ __align__(128) float s_rows[kRows][kPreGroup];
+    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
+    __shared__ ViewBlock sv;
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kPreGroup;
+    if (lt == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
+    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
+    __syncthreads();
+    const bool staged = g0 < stride;
+    if (lt == 0 && staged) {
+        // stride and g0 are multiples of 64: every row slice starts 256-byte aligned and spans a
+        // multiple of 256 bytes
+        const uint32_t cols = min(kPreGroup, stride - g0);
+        mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
+        for (int r = 0; r < kRowRest; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
+        mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
+        for (int r = kRowRest; r < kRows; ++r)
+            bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
+    }
+    if (staged) wait_staged(&s_bar[0], ctl);
+    auto attr = [&](int row) { return s_rows[row][lt]; };
+    const uint32_t g = g0 + lt;
+    if (g == 0) counts[n] = 0u;  // the N+1-th scan entry (cleared by renderer.js:826)
+    bool near_ok = false;
+    if (g < n)
+        near_ok = preprocess_gaussian(g, sv, tile, attr, [&]() { if (staged) wait_staged(&s_bar[1], ctl); }, rec, meta,
+                                      counts);
+    // every thread waits for the f_rest copies (those that evaluated SH already have): the CTA's
+    // shared memory must not be released while a bulk copy still writes into it
+    if (staged) wait_staged(&s_bar[1], ctl);
+    const int block_near = __syncthreads_count(near_ok);  // survivors of the near plane, for the statistics
+    if (lt == 0 && block_near) atomicAdd(&ctl->near_pass, (uint32_t)block_near);
+}
+
+// Several views of one scene: the CTA stages its slice of the attribute rows once and preprocesses
+// every view from shared memory, so the scene is read once per group of views.
+__global__ void __launch_bounds__(kPreGroup) k_preprocess_multi(const float* __restrict__ rows, uint32_t stride,
+                                                                uint32_t n, uint32_t tile, MultiViewFrames mv) {
+    __shared__ __align__(128) float s_rows[kRows][kPreGroup];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ ViewBlock sv;
+    const uint32_t lt = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kPreGroup;
+    const uint32_t g = g0 + lt;
+    if (lt == 0) mbar_init(&s_bar, 1);
+    __syncthreads();
+    if (lt == 0) {
+        // g0 < n <= stride; stride and g0 are multiples of 64: 256-byte aligned slices
+        const uint32_t cols = min(kPreGroup, stride - g0);
+        mbar_expect_tx(&s_bar, kRows * cols * 4u);
+        for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
+    }
+    {
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0)) {
+            if (++spins > kSpinLimit) {
+                if (lt == 0)
+                    for (uint32_t v = 0; v < mv.count; ++v) atomicOr(&mv.ctl[v]->status, kDevTimeout);
+                break;
+            }
+        }
+    }
+    auto attr = [&](int row) { return s_rows[row][lt]; };
+    for (uint32_t v = 0; v < mv.count; ++v) {
+        __syncthreads();  // sv is rewritten per view
+        if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(mv.view[v])[lt];
+        __syncthreads();
+        if (g == 0) mv.counts[v][n] = 0u;
+        bool near_ok = false;
+        if (g < n) near_ok = preprocess_gaussian(g, sv, tile, attr, []() {}, mv.rec[v], mv.meta[v], mv.counts[v]);
+        const int block_near = __syncthreads_count(near_ok);
+        if (lt == 0 && block_near) atomicAdd(&mv.ctl[v]->near_pass, (uint32_t)block_near);
+    }
 }
 
 // Attribute blocks of the packed layout (preprocess.wgsl:16-24): first row, floats per Gaussian, and
@@ -331,6 +385,12 @@ void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const Vie
                        float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s) {
     const uint32_t blocks = (n + kPreGroup - 1u) / kPreGroup;
     k_preprocess<<<blocks > 0 ? blocks : 1u, kPreGroup, 0, s>>>(rows, stride, n, view, tile, rec, meta, counts, ctl);
+}
+
+void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uint32_t tile, const MultiViewFrames& mv,
+                             cudaStream_t s) {
+    if (n == 0 || mv.count == 0) return;
+    k_preprocess_multi<<<(n + kPreGroup - 1u) / kPreGroup, kPreGroup, 0, s>>>(rows, stride, n, tile, mv);
 }
 
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
