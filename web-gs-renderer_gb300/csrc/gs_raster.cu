@@ -21,6 +21,9 @@
 //    been rejected by every pixel of the warp at "power < c_o" (or "power > 0"). Contributor counts
 //    are range positions, so skipping does not change them.
 //
+// Full residency (2048 threads per SM, 32 registers; the few spilled bytes cost less than the lost
+// warps did).
+//
 // CTA i renders tile order[i]: the tiles listed by decreasing range length, so the longest tiles
 // start first instead of forming the tail of the launch (with tiles in index order the clustered
 // scenes left about a third of the launch time to a few long tiles).
@@ -31,7 +34,7 @@ namespace gs {
 namespace {
 
 template <int TILE, int BATCH>
-__global__ void __launch_bounds__(TILE * TILE) k_raster(const uint32_t* __restrict__ ranges,
+__global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(const uint32_t* __restrict__ ranges,
                                                         const uint32_t* __restrict__ vals,
                                                         const float4* __restrict__ rec, uint32_t n,
                                                         const FrameCtl* __restrict__ ctl, uint32_t width,
