@@ -1,7 +1,8 @@
 """Build recipe of libwebgs.so (the CUDA kernels + C ABI) and of the CPU oracle library.
 
 Every CUDA translation unit is compiled for sm_103a only, in parallel, with -fmad=false so that
-the kernels keep the pinned fp32 semantics (fused multiply-adds only where written explicitly).
+the kernels keep the pinned fp32 semantics (fused multiply-adds only where written explicitly);
+the gradient and loss units, whose results are not pinned, contract freely.
 Host C++ is built with -ffp-contract=off for the same reason. Outputs stay in the tree:
   web-gs-renderer_gb300/lib/libwebgs.so
   oracle/liboracle.so            (test infrastructure; built beside the product, never linked into it)
@@ -29,6 +30,15 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills",
 ]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
+# Translation units whose results are not bit-pinned (gradients, the loss) may contract a*b+c into
+# fused multiply-adds.
+CONTRACTED = {"gs_preprocess_backward.cu", "gs_loss.cu"}
+
+
+def _nvcc_flags(src: Path) -> list[str]:
+    if src.name in CONTRACTED:
+        return [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS]
+    return NVCC_FLAGS
 
 
 def _nvcc() -> str:
@@ -64,7 +74,7 @@ def build_library(force: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers + [Path(__file__)]):
-            jobs.append([nvcc, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *_nvcc_flags(src), "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
     for src in sorted(CSRC.glob("*.cpp")):
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)

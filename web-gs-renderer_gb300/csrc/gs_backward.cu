@@ -1,17 +1,12 @@
-// gs_backward.cu -- gradients of the splat pipeline (no counterpart in the reference, which only
-// renders). Three kernels:
+// gs_backward.cu -- the raster half of the gradients of the splat pipeline (no counterpart in the
+// reference, which only renders):
 //   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
 //                         contributor, recomputing power and alpha bit for bit as the forward did
 //                         (same pinned arithmetic, the forward's warp cull box), recovering T by
 //                         division, and accumulating dL/d(pixel.xy, conic, opacity, colour) per
 //                         Gaussian: two pixels per lane, the warp reduces by shuffles, nine lanes
-//                         issue the atomics;
-//   k_preprocess_backward one thread per Gaussian: chain rule back through colour (SH), sigmoid,
-//                         conic inverse, 2D covariance J W Sigma W^T J^T, the rotation / scale
-//                         factorisation, and the projection, into the 59 attributes in the
-//                         packed input layout;
-//   k_preprocess_backward_multi  the same for several views of one scene, reading the scene once
-//                         and summing the views' gradients.
+//                         issue the atomics.
+// The preprocess half (2D gradients -> the 59 attributes) is in gs_preprocess_backward.cu.
 // Conventions: gradients flow through the fp32 RGB before quantization; culled Gaussians, skipped
 // pairs and splats after a pixel's termination get none; active clamps (alpha 0.99, colour >= 0)
 // pass none; where the frustum guard clamps t.x/t.z (t.y/t.z) no gradient flows through t.x (t.y),
@@ -98,23 +93,28 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
     const float og = b.y * G;
     const float alpha = fminf(kAlphaClamp, og);
     if (!(alpha >= kEpsilon)) return false;
+    // from here on only gradients are formed: fused multiply-adds are fine (the decisions above
+    // follow the forward's pinned arithmetic)
     const float Tb = __fdividef(p.T, 1.0f - alpha);  // transmittance in front of this splat
-    p.acc_r = p.last_a * p.last_r + (1.0f - p.last_a) * p.acc_r;
-    p.acc_g = p.last_a * p.last_g + (1.0f - p.last_a) * p.acc_g;
-    p.acc_b = p.last_a * p.last_b + (1.0f - p.last_a) * p.acc_b;
+    const float keep = 1.0f - p.last_a;
+    p.acc_r = __fmaf_rn(p.last_a, p.last_r, keep * p.acc_r);
+    p.acc_g = __fmaf_rn(p.last_a, p.last_g, keep * p.acc_g);
+    p.acc_b = __fmaf_rn(p.last_a, p.last_b, keep * p.acc_b);
     const float w = alpha * Tb;
-    g[6] += w * p.dr;
-    g[7] += w * p.dg;
-    g[8] += w * p.db;
-    const float dalpha = Tb * ((b.z - p.acc_r) * p.dr + (b.w - p.acc_g) * p.dg + (c.x - p.acc_b) * p.db);
+    g[6] = __fmaf_rn(w, p.dr, g[6]);
+    g[7] = __fmaf_rn(w, p.dg, g[7]);
+    g[8] = __fmaf_rn(w, p.db, g[8]);
+    const float dalpha =
+        Tb * __fmaf_rn(b.z - p.acc_r, p.dr, __fmaf_rn(b.w - p.acc_g, p.dg, (c.x - p.acc_b) * p.db));
     if (og <= kAlphaClamp) {
         const float gp = dalpha * og;  // dL/dpower
-        g[0] += gp * (-a.z * dx - a.w * dy);
-        g[1] += gp * (-b.x * dy - a.w * dx);
-        g[2] += gp * -0.5f * dx * dx;
-        g[3] += gp * -dx * dy;
-        g[4] += gp * -0.5f * dy * dy;
-        g[5] += dalpha * G;
+        const float gh = -0.5f * gp;
+        g[0] = __fmaf_rn(gp, __fmaf_rn(-a.z, dx, -(a.w * dy)), g[0]);
+        g[1] = __fmaf_rn(gp, __fmaf_rn(-b.x, dy, -(a.w * dx)), g[1]);
+        g[2] = __fmaf_rn(gh * dx, dx, g[2]);
+        g[3] = __fmaf_rn(-gp * dx, dy, g[3]);
+        g[4] = __fmaf_rn(gh * dy, dy, g[4]);
+        g[5] = __fmaf_rn(dalpha, G, g[5]);
     }
     p.last_a = alpha;
     p.last_r = b.z;
@@ -232,330 +232,6 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
     }
 }
 
-// ---- preprocess backward ---------------------------------------------------------------------------
-constexpr uint32_t kBwdGroup = 128;  // Gaussians (threads) per preprocess-backward CTA
-// Floats per staged attribute row: rows start 16-byte aligned (bulk-copy destinations) and the
-// packed write-out reads them with at most 4-way bank conflicts.
-constexpr uint32_t kBwdPitch = 132;
-
-// Chain rule of one visible Gaussian from its 2D gradients d2 = dL/d(pixel.xy, conic, opacity, rgb)
-// back to its 59 attributes. R_(row) reads an attribute, W_(row, v) emits its gradient; every W_ of a
-// row comes after the last R_ of that row, so W_ may overwrite the staged attribute in place.
-template <class RF, class WF, class SF>
-__device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const float* __restrict__ d2, RF R_, WF W_,
-                                                  SF sh_ready) {
-    const float gpx = d2[0], gpy = d2[1], gA = d2[2], gB = d2[3], gC = d2[4], go = d2[5];
-    const float p[3] = {R_(0), R_(1), R_(2)};
-    float pv[4], clip[4];
-    for (int i = 0; i < 4; ++i) {
-        pv[i] = sv.view[i] * p[0] + sv.view[4 + i] * p[1] + sv.view[8 + i] * p[2] + sv.view[12 + i];
-        clip[i] = sv.viewProj[i] * p[0] + sv.viewProj[4 + i] * p[1] + sv.viewProj[8 + i] * p[2] + sv.viewProj[12 + i];
-    }
-    const float wden = clip[3] + kSmallValue;
-    // rotation and scale
-    float s[3];
-    for (int i = 0; i < 3; ++i) s[i] = pinned_expf(R_(kRowScale + i));
-    const float qr[4] = {R_(kRowQuat + 1), R_(kRowQuat + 2), R_(kRowQuat + 3), R_(kRowQuat + 0)};  // (x, y, z, w)
-    const float qlen = sqrtf(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
-    const float q[4] = {qr[0] / qlen, qr[1] / qlen, qr[2] / qlen, qr[3] / qlen};
-    const float x = q[0], y = q[1], z = q[2], w = q[3];
-    float R[3][3];  // [row][col]
-    R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z);     R[0][2] = 2 * (x * z + w * y);
-    R[1][0] = 2 * (x * y + w * z);     R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
-    R[2][0] = 2 * (x * z - w * y);     R[2][1] = 2 * (y * z + w * x);     R[2][2] = 1 - 2 * (x * x + y * y);
-    float A[3][3], Sg[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) A[i][j] = R[i][j] * s[j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) Sg[i][j] = A[i][0] * A[j][0] + A[i][1] * A[j][1] + A[i][2] * A[j][2];
-    // 2D covariance
-    const float limx = kFrustumExtended * sv.tanFov[0], limy = kFrustumExtended * sv.tanFov[1];
-    const float tz = pv[2];
-    const float rxr = pv[0] / tz, ryr = pv[1] / tz;
-    const bool clampx = rxr < -limx || rxr > limx, clampy = ryr < -limy || ryr > limy;
-    const float tx = fminf(limx, fmaxf(-limx, rxr)) * tz, ty = fminf(limy, fmaxf(-limy, ryr)) * tz;
-    const float fxl = sv.focal[0], fyl = sv.focal[1];
-    const float J[2][3] = {{fxl / tz, 0.0f, -fxl * tx / (tz * tz)}, {0.0f, fyl / tz, -fyl * ty / (tz * tz)}};
-    float Wr[3][3];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) Wr[r][c] = sv.view[c * 4 + r];
-    float M[2][3];
-    for (int r = 0; r < 2; ++r)
-        for (int c = 0; c < 3; ++c) M[r][c] = J[r][0] * Wr[0][c] + J[r][1] * Wr[1][c] + J[r][2] * Wr[2][c];
-    float MS[2][3];
-    for (int r = 0; r < 2; ++r)
-        for (int c = 0; c < 3; ++c) MS[r][c] = M[r][0] * Sg[0][c] + M[r][1] * Sg[1][c] + M[r][2] * Sg[2][c];
-    const float ca = MS[0][0] * M[0][0] + MS[0][1] * M[0][1] + MS[0][2] * M[0][2] + 0.3f;
-    const float cb = MS[0][0] * M[1][0] + MS[0][1] * M[1][1] + MS[0][2] * M[1][2];
-    const float cc = MS[1][0] * M[1][0] + MS[1][1] * M[1][1] + MS[1][2] * M[1][2] + 0.3f;
-    const float det = ca * cc - cb * cb, det2 = det * det;
-    // conic -> (a, b, c)
-    const float ga = gA * (-cc * cc / det2) + gB * (cb * cc / det2) + gC * (-cb * cb / det2);
-    const float gb = gA * (2 * cb * cc / det2) + gB * (-(ca * cc + cb * cb) / det2) + gC * (2 * ca * cb / det2);
-    const float gc = gA * (-cb * cb / det2) + gB * (cb * ca / det2) + gC * (-ca * ca / det2);
-    const float G2[2][2] = {{ga, 0.5f * gb}, {0.5f * gb, gc}};
-    // dL/dSigma = M^T G2 M ; dL/dM = 2 G2 M Sigma
-    float GM[2][3];
-    for (int r = 0; r < 2; ++r)
-        for (int c = 0; c < 3; ++c) GM[r][c] = G2[r][0] * M[0][c] + G2[r][1] * M[1][c];
-    float gS[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) gS[i][j] = M[0][i] * GM[0][j] + M[1][i] * GM[1][j];
-    float gM[2][3];
-    for (int r = 0; r < 2; ++r)
-        for (int c = 0; c < 3; ++c) gM[r][c] = 2.0f * (G2[r][0] * MS[0][c] + G2[r][1] * MS[1][c]);
-    // dL/dJ = dL/dM Wr^T
-    float gJ[2][3];
-    for (int r = 0; r < 2; ++r)
-        for (int k = 0; k < 3; ++k) gJ[r][k] = gM[r][0] * Wr[k][0] + gM[r][1] * Wr[k][1] + gM[r][2] * Wr[k][2];
-    const float tz2 = tz * tz, tz3 = tz2 * tz;
-    float gpv[3];
-    gpv[0] = clampx ? 0.0f : gJ[0][2] * (-fxl / tz2);
-    gpv[1] = clampy ? 0.0f : gJ[1][2] * (-fyl / tz2);
-    gpv[2] = gJ[0][0] * (-fxl / tz2) + gJ[0][2] * (2.0f * fxl * tx / tz3) + gJ[1][1] * (-fyl / tz2) +
-             gJ[1][2] * (2.0f * fyl * ty / tz3);
-    float gp[3];
-    for (int i = 0; i < 3; ++i) gp[i] = Wr[0][i] * gpv[0] + Wr[1][i] * gpv[1] + Wr[2][i] * gpv[2];
-    // pixel position -> clip -> p
-    const float gndx = gpx * sv.textureSize[0] * 0.5f, gndy = gpy * sv.textureSize[1] * 0.5f;
-    const float gcx = gndx / wden, gcy = gndy / wden, gcw = -(gndx * clip[0] + gndy * clip[1]) / (wden * wden);
-    for (int i = 0; i < 3; ++i) gp[i] += sv.viewProj[i * 4 + 0] * gcx + sv.viewProj[i * 4 + 1] * gcy + sv.viewProj[i * 4 + 3] * gcw;
-    // colour (SH)
-    float v[3] = {p[0] - sv.cameraPos[0], p[1] - sv.cameraPos[1], p[2] - sv.cameraPos[2]};
-    const float vlen = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    const float dx_ = v[0] / vlen, dy_ = v[1] / vlen, dz_ = v[2] / vlen;
-    const float xx = dx_ * dx_, yy = dy_ * dy_, zz = dz_ * dz_;
-    float Y[16];
-    Y[0] = kShC0;
-    Y[1] = -kShC1 * dy_;
-    Y[2] = kShC1 * dz_;
-    Y[3] = -kShC1 * dx_;
-    Y[4] = kShC2_0 * dx_ * dy_;
-    Y[5] = kShC2_1 * dy_ * dz_;
-    Y[6] = kShC2_2 * (2 * zz - xx - yy);
-    Y[7] = kShC2_3 * dx_ * dz_;
-    Y[8] = kShC2_4 * (xx - yy);
-    Y[9] = kShC3_0 * dy_ * (3 * xx - yy);
-    Y[10] = kShC3_1 * dx_ * dy_ * dz_;
-    Y[11] = kShC3_2 * dy_ * (4 * zz - xx - yy);
-    Y[12] = kShC3_3 * dz_ * (2 * zz - 3 * xx - 3 * yy);
-    Y[13] = kShC3_4 * dx_ * (4 * zz - xx - yy);
-    Y[14] = kShC3_5 * dz_ * (xx - yy);
-    Y[15] = kShC3_6 * dx_ * (xx - 3 * yy);
-    sh_ready();  // the f_rest rows arrive on their own barrier
-    float gcol[3];
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-        float raw = Y[0] * R_(kRowDc + ch);
-#pragma unroll
-        for (int k = 1; k < 16; ++k) raw += Y[k] * R_(kRowRest + (k - 1) + 15 * ch);
-        raw += 0.5f;
-        gcol[ch] = raw < 0.0f ? 0.0f : d2[6 + ch];
-    }
-    float wsh[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            const int row = k == 0 ? kRowDc + ch : kRowRest + (k - 1) + 15 * ch;
-            acc += R_(row) * gcol[ch];
-            W_(row, Y[k] * gcol[ch]);
-        }
-        wsh[k] = acc;
-    }
-    float gdx = 0, gdy = 0, gdz = 0;
-    gdy += -kShC1 * wsh[1];
-    gdz += kShC1 * wsh[2];
-    gdx += -kShC1 * wsh[3];
-    gdx += kShC2_0 * dy_ * wsh[4];           gdy += kShC2_0 * dx_ * wsh[4];
-    gdy += kShC2_1 * dz_ * wsh[5];           gdz += kShC2_1 * dy_ * wsh[5];
-    gdx += -2 * kShC2_2 * dx_ * wsh[6];      gdy += -2 * kShC2_2 * dy_ * wsh[6];      gdz += 4 * kShC2_2 * dz_ * wsh[6];
-    gdx += kShC2_3 * dz_ * wsh[7];           gdz += kShC2_3 * dx_ * wsh[7];
-    gdx += 2 * kShC2_4 * dx_ * wsh[8];       gdy += -2 * kShC2_4 * dy_ * wsh[8];
-    gdx += 6 * kShC3_0 * dx_ * dy_ * wsh[9]; gdy += kShC3_0 * (3 * xx - 3 * yy) * wsh[9];
-    gdx += kShC3_1 * dy_ * dz_ * wsh[10];    gdy += kShC3_1 * dx_ * dz_ * wsh[10];    gdz += kShC3_1 * dx_ * dy_ * wsh[10];
-    gdx += -2 * kShC3_2 * dx_ * dy_ * wsh[11]; gdy += kShC3_2 * (4 * zz - xx - 3 * yy) * wsh[11]; gdz += 8 * kShC3_2 * dy_ * dz_ * wsh[11];
-    gdx += -6 * kShC3_3 * dx_ * dz_ * wsh[12]; gdy += -6 * kShC3_3 * dy_ * dz_ * wsh[12]; gdz += kShC3_3 * (6 * zz - 3 * xx - 3 * yy) * wsh[12];
-    gdx += kShC3_4 * (4 * zz - 3 * xx - yy) * wsh[13]; gdy += -2 * kShC3_4 * dx_ * dy_ * wsh[13]; gdz += 8 * kShC3_4 * dx_ * dz_ * wsh[13];
-    gdx += 2 * kShC3_5 * dx_ * dz_ * wsh[14]; gdy += -2 * kShC3_5 * dy_ * dz_ * wsh[14]; gdz += kShC3_5 * (xx - yy) * wsh[14];
-    gdx += kShC3_6 * (3 * xx - 3 * yy) * wsh[15]; gdy += -6 * kShC3_6 * dx_ * dy_ * wsh[15];
-    const float ddot = gdx * dx_ + gdy * dy_ + gdz * dz_;
-    gp[0] += (gdx - dx_ * ddot) / vlen;
-    gp[1] += (gdy - dy_ * ddot) / vlen;
-    gp[2] += (gdz - dz_ * ddot) / vlen;
-    for (int i = 0; i < 3; ++i) W_(kRowPos + i, gp[i]);
-    // opacity logit
-    const float op = 1.0f / (1.0f + pinned_expf(-R_(kRowOpacity)));
-    W_(kRowOpacity, go * op * (1.0f - op));
-    // Sigma = A A^T -> A -> (R, s) -> (quaternion, log-scale)
-    float gAm[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            gAm[i][j] = (gS[i][0] + gS[0][i]) * A[0][j] + (gS[i][1] + gS[1][i]) * A[1][j] + (gS[i][2] + gS[2][i]) * A[2][j];
-    float gR[3][3];
-    for (int j = 0; j < 3; ++j) {
-        float gs = 0.0f;
-        for (int i = 0; i < 3; ++i) {
-            gs += gAm[i][j] * R[i][j];
-            gR[i][j] = gAm[i][j] * s[j];
-        }
-        W_(kRowScale + j, gs * s[j]);
-    }
-    float gq[4];
-    gq[0] = gR[1][0] * 2 * y + gR[2][0] * 2 * z + gR[0][1] * 2 * y + gR[1][1] * -4 * x + gR[2][1] * 2 * w +
-            gR[0][2] * 2 * z + gR[1][2] * -2 * w + gR[2][2] * -4 * x;
-    gq[1] = gR[0][0] * -4 * y + gR[1][0] * 2 * x + gR[2][0] * -2 * w + gR[0][1] * 2 * x + gR[2][1] * 2 * z +
-            gR[0][2] * 2 * w + gR[1][2] * 2 * z + gR[2][2] * -4 * y;
-    gq[2] = gR[0][0] * -4 * z + gR[1][0] * 2 * w + gR[2][0] * 2 * x + gR[0][1] * -2 * w + gR[1][1] * -4 * z +
-            gR[2][1] * 2 * y + gR[0][2] * 2 * x + gR[1][2] * 2 * y;
-    gq[3] = gR[1][0] * 2 * z + gR[2][0] * -2 * y + gR[0][1] * -2 * z + gR[2][1] * 2 * x + gR[0][2] * 2 * y +
-            gR[1][2] * -2 * x;
-    const float qd = gq[0] * q[0] + gq[1] * q[1] + gq[2] * q[2] + gq[3] * q[3];
-    W_(kRowQuat + 0, (gq[3] - q[3] * qd) / qlen);  // stored rot_0 = w
-    W_(kRowQuat + 1, (gq[0] - q[0] * qd) / qlen);
-    W_(kRowQuat + 2, (gq[1] - q[1] * qd) / qlen);
-    W_(kRowQuat + 3, (gq[2] - q[2] * qd) / qlen);
-}
-
-// One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
-// residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of the 59
-// attribute rows in shared memory with bulk copies (as the forward preprocess does): the geometry rows
-// on one mbarrier and the 45 f_rest rows on another, so the geometric part of the chain rule overlaps
-// the arrival of the SH coefficients. The gradients replace the staged attributes in shared memory
-// and the CTA writes its slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest
-// blocks, the layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros.
-__global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
-                                                                   uint32_t n, const ViewBlock* __restrict__ vb,
-                                                                   const uint32_t* __restrict__ counts,
-                                                                   const float* __restrict__ grad2d,
-                                                                   float* __restrict__ out, uint32_t* status) {
-    __shared__ __align__(128) float s_rows[kRows][kBwdPitch];
-    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
-    __shared__ ViewBlock sv;
-    const uint32_t lt = threadIdx.x;
-    const uint32_t g0 = blockIdx.x * kBwdGroup;
-    const uint32_t g = g0 + lt;
-    const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
-    const bool vis = g < n && counts[g] != 0u;
-    if (lt == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
-    }
-    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
-    const int any = __syncthreads_or(vis);
-    // bounded wait: on expiry the timeout is recorded and the kernel goes on with what is there
-    auto wait_bar = [&](uint64_t* bar) {
-        uint32_t spins = 0;
-        while (!mbar_try_wait(bar, 0)) {
-            if (++spins > kSpinLimit) {
-                if (lt == 0 && status) atomicOr(status, kDevTimeout);
-                break;
-            }
-        }
-    };
-    if (any) {
-        if (lt == 0) {
-            // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and
-            // spans a multiple of 256 bytes (g0 < n <= stride)
-            const uint32_t cols = min(kBwdGroup, stride - g0);
-            mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
-            for (int r = 0; r < kRowRest; ++r)
-                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
-            mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
-            for (int r = kRowRest; r < kRows; ++r)
-                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
-        }
-        wait_bar(&s_bar[0]);
-        if (vis) {
-            auto R_ = [&](int row) { return s_rows[row][lt]; };
-            auto W_ = [&](int row, float v) { s_rows[row][lt] = v; };
-            backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_, [&]() { wait_bar(&s_bar[1]); });
-        } else {
-            // every thread waits for the f_rest copies before it overwrites its column or leaves: no
-            // bulk copy may still write into shared memory that is reused or released
-            wait_bar(&s_bar[1]);
-            for (int r = 0; r < kRows; ++r) s_rows[r][lt] = 0.0f;
-        }
-    }
-    __syncthreads();
-    // the CTA's Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute block
-    struct Block { uint32_t row, width, base; };
-    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
-                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
-#pragma unroll
-    for (int bi = 0; bi < 6; ++bi) {
-        const Block bk = blocks[bi];
-        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
-        const uint32_t total = bk.width * cnt;
-        for (uint32_t i = lt; i < total; i += kBwdGroup)
-            dst[i] = any ? s_rows[bk.row + i % bk.width][i / bk.width] : 0.0f;
-    }
-}
-
-// Several views of one scene: one thread per Gaussian stages the 59 attribute rows once (bulk copies)
-// and runs the chain rule for every view that sees the Gaussian, summing the views' gradients in a
-// shared-memory tile of its own column; the CTA then writes its slice of the packed layout with
-// coalesced stores (stored, or added to what an earlier group of views wrote). The scene is read
-// once per batch instead of once per view, and no atomics, clearing or transpose pass are needed.
-__global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward_multi(const float* __restrict__ rows,
-                                                                         uint32_t stride, uint32_t n,
-                                                                         MultiViewGrads mv, float* __restrict__ out,
-                                                                         int add, uint32_t* status) {
-    extern __shared__ __align__(128) float s_dyn[];
-    float(*s_rows)[kBwdPitch] = reinterpret_cast<float(*)[kBwdPitch]>(s_dyn);
-    float(*s_grad)[kBwdPitch] = reinterpret_cast<float(*)[kBwdPitch]>(s_dyn + kRows * kBwdPitch);
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ ViewBlock sv;
-    const uint32_t lt = threadIdx.x;
-    const uint32_t g0 = blockIdx.x * kBwdGroup;
-    const uint32_t g = g0 + lt;
-    const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
-    uint32_t seen = 0u;                           // views that see this Gaussian (bit per view)
-    for (uint32_t v = 0; v < mv.count; ++v)
-        if (g < n && mv.counts[v][g] != 0u) seen |= 1u << v;
-    if (lt == 0) mbar_init(&s_bar, 1);
-    for (int r = 0; r < kRows; ++r) s_grad[r][lt] = 0.0f;
-    const int any = __syncthreads_or(seen != 0u);
-    if (any) {
-        if (lt == 0) {
-            // stride and g0 are multiples of 64 floats: 256-byte aligned slices of 256-byte multiples
-            const uint32_t cols = min(kBwdGroup, stride - g0);
-            mbar_expect_tx(&s_bar, kRows * cols * 4u);
-            for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
-        }
-        uint32_t spins = 0;
-        while (!mbar_try_wait(&s_bar, 0)) {  // every thread waits: no copy may outlive the CTA
-            if (++spins > kSpinLimit) {
-                if (lt == 0 && status) atomicOr(status, kDevTimeout);
-                break;
-            }
-        }
-        auto R_ = [&](int row) { return s_rows[row][lt]; };
-        auto W_ = [&](int row, float val) { s_grad[row][lt] += val; };
-        for (uint32_t v = 0; v < mv.count; ++v) {
-            __syncthreads();  // sv is rewritten per view
-            if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(mv.view[v])[lt];
-            __syncthreads();
-            if (seen & (1u << v)) backward_gaussian(sv, mv.grad2d[v] + (size_t)9 * g, R_, W_, []() {});
-        }
-    }
-    __syncthreads();
-    struct Block { uint32_t row, width, base; };
-    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
-                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
-#pragma unroll
-    for (int bi = 0; bi < 6; ++bi) {
-        const Block bk = blocks[bi];
-        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
-        const uint32_t total = bk.width * cnt;
-        for (uint32_t i = lt; i < total; i += kBwdGroup) {
-            const float val = s_grad[bk.row + i % bk.width][i / bk.width];
-            dst[i] = add ? dst[i] + val : val;
-        }
-    }
-}
-
 template <int TILE>
 void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
                      const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
@@ -583,28 +259,6 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
         launch_bwd_tile<32>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
     else
         launch_bwd_tile<16>(batch, ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, final_t, n_contrib, dl_drgb, grad2d, order, s);
-}
-
-size_t preprocess_backward_multi_smem() { return (size_t)2 * kRows * kBwdPitch * sizeof(float); }
-
-void configure_backward_kernels() {
-    cudaFuncSetAttribute(k_preprocess_backward_multi, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)preprocess_backward_multi_smem());
-}
-
-void launch_preprocess_backward_multi(const float* rows, uint32_t stride, uint32_t n, const MultiViewGrads& mv,
-                                      float* out, bool add, uint32_t* status, cudaStream_t s) {
-    if (n == 0 || mv.count == 0) return;
-    k_preprocess_backward_multi<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, preprocess_backward_multi_smem(), s>>>(
-        rows, stride, n, mv, out, add ? 1 : 0, status);
-}
-
-void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
-                                cudaStream_t s) {
-    if (n == 0) return;
-    k_preprocess_backward<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, 0, s>>>(rows, stride, n, view, counts,
-                                                                                grad2d, out, status);
 }
 
 }  // namespace gs

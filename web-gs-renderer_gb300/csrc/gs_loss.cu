@@ -7,9 +7,8 @@
 // halo staged in shared memory (both separable passes happen there):
 //   k_ssim_fwd  moments -> SSIM map -> its three partials (to global) + per-block SSIM and L1 sums;
 //   k_ssim_bwd  blurred partials + the L1 term -> dL/dx.
-// Images are H x W x 3 (pixel-interleaved). The library is compiled without multiply-add
-// contraction (the splat kernels need it so); the loss is not bit-pinned, so its filters use
-// explicit fused multiply-adds.
+// Images are H x W x 3 (pixel-interleaved). The loss is not bit-pinned: this file is built with
+// multiply-add contraction and its filters use fused multiply-adds.
 #include <cmath>
 
 #include "gs_kernels.h"
