@@ -139,9 +139,10 @@ uint32_t gs_scene_count(const gs_scene* scene);
 
 /* Replaces Renderer.execute() (renderer.js:481-508) with the passes of renderer.js:822-932:
  * preprocess, offset scan, emit, device-side sizing, radix sort, tile ranges, raster; the blit
- * (blit.wgsl) becomes `out`. Host outputs: returns after the image is on the host. Device
- * outputs: stream-ordered, returns after launch. Returns GS_ERR_OVERFLOW (outputs written) when
- * the instance count exceeded the budget. */
+ * (blit.wgsl) becomes `out`. Host outputs: returns after the image is on the host; rgba8 and rgb
+ * buffers in pinned (page-locked or registered) host memory are written by the raster directly,
+ * pageable ones through a staging copy. Device outputs: stream-ordered, returns after launch.
+ * Returns GS_ERR_OVERFLOW (outputs written) when the instance count exceeded the budget. */
 int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs_image* out);
 
 /* One view of a batch: a scene, its 176-byte view block and its outputs. */

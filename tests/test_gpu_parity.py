@@ -155,6 +155,39 @@ def test_needle_splats_parity(gpu_ctx, seed):
     assert_frame_parity(g, o)
 
 
+def test_pinned_host_output_is_written_directly(gpu_ctx):
+    """Host images in pinned memory are written by the raster itself (no staging copy): same bytes
+    as through the pageable path, for a single frame and for a batch."""
+    import ctypes as C
+
+    import torch
+
+    from webgs import _abi
+
+    packed = W.SMALL_SCENE.build()
+    view = W.SMALL_CAMERA.view()
+    scene = gpu_ctx.upload(packed, W.SMALL_SCENE.count)
+    try:
+        ref = gpu_ctx.forward(scene, view, rgba8=True, rgb=True)
+        h8 = torch.zeros(512 * 512 * 4, dtype=torch.uint8, pin_memory=True)
+        hrgb = torch.zeros(512 * 512 * 3, dtype=torch.float32, pin_memory=True)
+        img = _abi.Image(webgs.GS_MEM_HOST, h8.data_ptr(), hrgb.data_ptr(), None, None)
+        assert webgs.library().gs_forward(gpu_ctx.handle, scene.handle, C.byref(view), C.byref(img)) == 0
+        np.testing.assert_array_equal(h8.numpy().reshape(512, 512, 4), ref["rgba8"])
+        np.testing.assert_array_equal(hrgb.numpy().reshape(512, 512, 3).view(np.uint32), ref["rgb"].view(np.uint32))
+        arr = (_abi.BatchView * 2)()
+        outs = [torch.zeros(512 * 512 * 4, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+        for k in range(2):
+            arr[k].scene = scene.handle
+            arr[k].view = view
+            arr[k].out = _abi.Image(webgs.GS_MEM_HOST, outs[k].data_ptr(), None, None, None)
+        assert webgs.library().gs_forward_batch(gpu_ctx.handle, arr, 2) == 0
+        for o in outs:
+            np.testing.assert_array_equal(o.numpy().reshape(512, 512, 4), ref["rgba8"])
+    finally:
+        scene.close()
+
+
 def test_repeat_frames_are_deterministic(gpu_ctx):
     packed = W.SceneSpec(30_000, 10, 0).build()
     view = W.CameraSpec((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 60.0, 320, 240).view()

@@ -72,6 +72,7 @@ struct Frame {
     uint32_t n = 0, width = 0, height = 0, tiles_x = 0, tiles_y = 0, passes = 0, max_instance = 0;
     int sorted_buf = 0;
     bool valid = false;
+    bool direct_rgba8 = false, direct_rgb = false;  // the raster writes the caller's host buffer itself
 
     cudaError_t init(cudaStream_t s) {
         cudaError_t e = ctl.reserve(1);
@@ -244,13 +245,32 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
 
 // Raster outputs of a frame: caller device buffers, or the frame's own buffers for host outputs and
 // for the state a differentiable context keeps (final T and last contributor).
+// The device address of a host buffer the GPU can write directly (pinned / registered memory), or
+// null for pageable memory, which is reached through a staging copy.
+void* mapped_host(const void* p) {
+    cudaPointerAttributes attr{};
+    if (!p || cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 RasterOut raster_out(const gs_ctx* ctx, Frame& f, const gs_image* out) {
     const bool dev = out && out->location == GS_MEM_DEVICE;
     const bool keep = (ctx->cfg.flags & GS_FLAG_DIFFERENTIABLE) != 0;
     RasterOut ro{};
+    f.direct_rgba8 = f.direct_rgb = false;
     if (out) {
-        ro.rgba8 = out->rgba8 ? (dev ? reinterpret_cast<uint32_t*>(out->rgba8) : f.rgba8.p) : nullptr;
-        ro.rgb = out->rgb ? (dev ? out->rgb : f.rgb.p) : nullptr;
+        // host images in pinned memory are written by the raster over the host link (no staging copy)
+        void* h8 = !dev && out->rgba8 ? mapped_host(out->rgba8) : nullptr;
+        void* hrgb = !dev && out->rgb ? mapped_host(out->rgb) : nullptr;
+        f.direct_rgba8 = h8 != nullptr;
+        f.direct_rgb = hrgb != nullptr;
+        ro.rgba8 = out->rgba8 ? (dev ? reinterpret_cast<uint32_t*>(out->rgba8)
+                                     : h8 ? static_cast<uint32_t*>(h8) : f.rgba8.p)
+                              : nullptr;
+        ro.rgb = out->rgb ? (dev ? out->rgb : hrgb ? static_cast<float*>(hrgb) : f.rgb.p) : nullptr;
     }
     if (keep) {
         ro.final_t = f.final_t.p;
@@ -319,8 +339,8 @@ int copy_outputs(gs_ctx* ctx, Frame& f, const gs_image* out, cudaStream_t s) {
         }
         return GS_OK;
     }
-    if (out->rgba8) GS_CK(cudaMemcpyAsync(out->rgba8, f.rgba8.p, pix * 4, cudaMemcpyDeviceToHost, s));
-    if (out->rgb) GS_CK(cudaMemcpyAsync(out->rgb, f.rgb.p, pix * 12, cudaMemcpyDeviceToHost, s));
+    if (out->rgba8 && !f.direct_rgba8) GS_CK(cudaMemcpyAsync(out->rgba8, f.rgba8.p, pix * 4, cudaMemcpyDeviceToHost, s));
+    if (out->rgb && !f.direct_rgb) GS_CK(cudaMemcpyAsync(out->rgb, f.rgb.p, pix * 12, cudaMemcpyDeviceToHost, s));
     if (out->final_t) GS_CK(cudaMemcpyAsync(out->final_t, f.final_t.p, pix * 4, cudaMemcpyDeviceToHost, s));
     if (out->n_contrib) GS_CK(cudaMemcpyAsync(out->n_contrib, f.n_contrib.p, pix * 4, cudaMemcpyDeviceToHost, s));
     return GS_OK;
