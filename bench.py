@@ -560,7 +560,7 @@ def batched_forward(steps, warmup, local_rank) -> dict:
 
 def batched_fwd_bwd(steps, warmup, local_rank) -> dict:
     """One 3M-Gaussian scene (seed 6, 128 clusters, 40^3 box), 8 cameras at 1920x1080: one batched
-    forward + 8 losses + one batched backward (gradients summed with FP32 atomics) vs 8 sequential
+    forward + 8 losses + one batched backward (gradients of the 8 views summed) vs 8 sequential
     forward + loss + backward calls."""
     import ctypes as C
 

@@ -171,7 +171,8 @@ int gs_get_debug(gs_ctx* ctx, const gs_debug* dbg);
 int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float* grad_packed, int32_t location);
 
 /* Backward of views 0..count-1 of the last gs_forward_batch, all of `scene`: dl_drgb[i] is view i's
- * dL/drgb; the gradients of all views are summed (FP32 atomics) into grad_packed. */
+ * dL/drgb; the gradients of all views are summed into grad_packed (the raster backwards run concurrently,
+ * then one pass over the scene per group of up to 16 views adds their attribute gradients). */
 int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
                       float* grad_packed, int32_t location);
 
