@@ -19,8 +19,12 @@ namespace gs {
 // checks are needed and 2^n (n >= -9) is applied as one exact power-of-two factor, which gives the
 // same bits as pinned_expf's two-factor scaling. o = 0 (cut-off +inf) never gets here; for a NaN
 // opacity the product o * exp(.) is NaN whatever this returns, as with pinned_expf.
+// n = rint(x * log2 e) comes from the 1.5 * 2^23 shift: for |x log2 e| < 2^22 the sum rounds to an
+// integer, to nearest even, exactly as rintf does, and its bits also give 2^n (no float-to-int
+// conversion); the result is bit-identical to the rintf form.
 __device__ __forceinline__ float raster_expf(float x) {
-    const float n = rintf(__fmul_rn(x, 0x1.715476p+0f));
+    const float t = __fadd_rn(__fmul_rn(x, 0x1.715476p+0f), 12582912.0f);
+    const float n = __fadd_rn(t, -12582912.0f);
     float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
     r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
     float p = 0x1.a01a02p-13f;
@@ -31,7 +35,7 @@ __device__ __forceinline__ float raster_expf(float x) {
     p = __fmaf_rn(p, r, 0.5f);
     p = __fmaf_rn(p, r, 1.0f);
     p = __fmaf_rn(p, r, 1.0f);
-    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
+    return __fmul_rn(p, __int_as_float((__float_as_int(t) + 127) << 23));
 }
 
 __device__ __forceinline__ bool finite_f(float v) { return fabsf(v) <= 3.0e38f; }
