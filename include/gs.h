@@ -184,6 +184,12 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
 int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
                 uint32_t iters, gs_config* best, float* best_ms);
 
+/* The same sweep over a batch of several scenes: packed[s] / counts[s] are the scenes (host, packed
+ * layout), view i renders scene view_scene[i] (NULL: every view renders scene 0). */
+int gs_autotune_scenes(const gs_config* base, const float* const* packed, const uint32_t* counts, uint32_t n_scenes,
+                       const gs_view* views, const uint32_t* view_scene, uint32_t n_views, uint32_t iters,
+                       gs_config* best, float* best_ms);
+
 /* Loss of the differentiation workload (no counterpart in the reference): L = mean|rgb - target| +
  * lambda * (1 - mean SSIM), SSIM per channel with an 11x11 Gaussian window (sigma 1.5), zero padding,
  * C1 = 0.01^2, C2 = 0.03^2; images H x W x 3. *loss (host, may be NULL) receives L; dl_drgb (may be

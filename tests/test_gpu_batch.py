@@ -71,3 +71,15 @@ def test_autotune_picks_a_valid_configuration():
     assert cfg["raster_batch"] in (32, 64, 128, 256) and cfg["sort_block"] in (2048, 4096) and ms > 0
     with webgs.Context(**cfg) as ctx:  # the pick is a configuration a context accepts
         assert ctx.config.sort_block == cfg["sort_block"]
+
+
+def test_autotune_over_several_scenes():
+    specs = [W.SceneSpec(8_000, 7, 0), W.SceneSpec(12_000, 8, 1, 16, 8.0)]
+    scenes = [(s.build(), s.count) for s in specs]
+    views = [W.CameraSpec((0.0, 0.0, -4.0), (0, 0, 0), 60.0, 160, 120).view(),
+             W.CameraSpec((0.0, 0.5, -6.0), (0, 0, 0), 60.0, 200, 100).view(),
+             W.CameraSpec((1.0, 0.0, -5.0), (0, 0, 0), 70.0, 96, 96).view()]
+    cfg, ms = webgs.autotune_scenes(scenes, views, [0, 1, 1], iters=1)
+    assert cfg["tile_size"] in (8, 16, 32) and cfg["digit_bits"] in (4, 8) and ms > 0
+    with pytest.raises(webgs.GsError):
+        webgs.autotune_scenes(scenes, views, [0, 1, 2], iters=1)  # scene index out of range

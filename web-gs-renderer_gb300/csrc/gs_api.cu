@@ -998,9 +998,14 @@ int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t
 }
 
 // ---- autotuner -------------------------------------------------------------------------------------
-int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
-                uint32_t iters, gs_config* best, float* best_ms) {
-    if (!packed || !views || n_views == 0 || !best) return GS_ERR_INVALID;
+int gs_autotune_scenes(const gs_config* base, const float* const* packed, const uint32_t* counts, uint32_t n_scenes,
+                       const gs_view* views, const uint32_t* view_scene, uint32_t n_views, uint32_t iters,
+                       gs_config* best, float* best_ms) {
+    if (!packed || !counts || n_scenes == 0 || !views || n_views == 0 || !best) return GS_ERR_INVALID;
+    for (uint32_t s = 0; s < n_scenes; ++s)
+        if (!packed[s] && counts[s]) return GS_ERR_INVALID;
+    for (uint32_t i = 0; i < n_views; ++i)
+        if (view_scene && view_scene[i] >= n_scenes) return GS_ERR_INVALID;
     gs_config b;
     gs_config_default(&b);
     if (base) b = *base;
@@ -1022,36 +1027,41 @@ int gs_autotune(const gs_config* base, const float* packed, uint32_t count, cons
                 c.flags &= ~(GS_FLAG_PROFILE | GS_FLAG_DIFFERENTIABLE);
                 gs_ctx* ctx = nullptr;
                 if (gs_ctx_create(&c, &ctx) != GS_OK) return GS_ERR_CUDA;
-                gs_scene* sc = nullptr;
-                int rc = gs_scene_upload(ctx, packed, count, GS_MEM_HOST, &sc);
+                std::vector<gs_scene*> scs(n_scenes, nullptr);
+                int rc = GS_OK;
+                for (uint32_t s = 0; rc == GS_OK && s < n_scenes; ++s)
+                    rc = gs_scene_upload(ctx, packed[s], counts[s], GS_MEM_HOST, &scs[s]);
                 std::vector<gs_batch_view> bv(n_views);
                 std::vector<uint32_t*> imgs(n_views, nullptr);
                 for (uint32_t i = 0; rc == GS_OK && i < n_views; ++i) {
                     const size_t pix = (size_t)views[i].texture_size[0] * (size_t)views[i].texture_size[1];
                     if (cudaMalloc(&imgs[i], pix * 4) != cudaSuccess) rc = GS_ERR_OOM;
-                    bv[i].scene = sc;
+                    bv[i].scene = scs[view_scene ? view_scene[i] : 0];
                     bv[i].view = views[i];
                     bv[i].out = gs_image{GS_MEM_DEVICE, reinterpret_cast<uint8_t*>(imgs[i]), nullptr, nullptr, nullptr};
                 }
                 float ms = 0.0f;
                 if (rc == GS_OK) {
-                    for (int w = 0; w < 2 && rc == GS_OK; ++w) rc = gs_forward_batch(ctx, bv.data(), n_views);
+                    for (int w = 0; w < 2 && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++w)
+                        rc = gs_forward_batch(ctx, bv.data(), n_views);
                     cudaEvent_t e0, e1;
                     cudaEventCreate(&e0);
                     cudaEventCreate(&e1);
                     cudaEventRecord(e0, ctx->stream);
-                    for (uint32_t k = 0; k < std::max(iters, 1u) && rc == GS_OK; ++k) rc = gs_forward_batch(ctx, bv.data(), n_views);
+                    for (uint32_t k = 0; k < std::max(iters, 1u) && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++k)
+                        rc = gs_forward_batch(ctx, bv.data(), n_views);
                     cudaEventRecord(e1, ctx->stream);
                     cudaEventSynchronize(e1);
                     cudaEventElapsedTime(&ms, e0, e1);
                     ms /= (float)std::max(iters, 1u);
                     cudaEventDestroy(e0);
                     cudaEventDestroy(e1);
-                    if (rc == GS_OK) rc = gs_ctx_synchronize(ctx);
+                    if (rc == GS_OK || rc == GS_ERR_OVERFLOW) rc = gs_ctx_synchronize(ctx);
                 }
                 for (uint32_t* p : imgs)
                     if (p) cudaFree(p);
-                if (sc) gs_scene_destroy(sc);
+                for (gs_scene* sc : scs)
+                    if (sc) gs_scene_destroy(sc);
                 gs_ctx_destroy(ctx);
                 if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return rc;
                 if (ms < best_t) {
@@ -1063,6 +1073,12 @@ int gs_autotune(const gs_config* base, const float* packed, uint32_t count, cons
     *best = best_c;
     if (best_ms) *best_ms = best_t;
     return GS_OK;
+}
+
+int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
+                uint32_t iters, gs_config* best, float* best_ms) {
+    if (!packed && count) return GS_ERR_INVALID;
+    return gs_autotune_scenes(base, &packed, &count, 1, views, nullptr, n_views, iters, best, best_ms);
 }
 
 // ---- building blocks -------------------------------------------------------------------------------

@@ -195,6 +195,26 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
     W_(kRowQuat + 3, (gq[2] - q[2] * qd) / qlen);
 }
 
+// Writes the CTA's gradient tile (one column per Gaussian, rows as the scene layout) to its slice of
+// the packed layout: the Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute
+// block, so every block is one coalesced run. zero: write zeros; add: add to what `out` holds.
+__device__ __forceinline__ void write_packed(const float (*tile)[kBwdPitch], float* __restrict__ out, uint32_t n,
+                                             uint32_t g0, uint32_t cnt, bool zero, bool add) {
+    struct Block { uint32_t row, width, base; };
+    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
+                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
+#pragma unroll
+    for (int bi = 0; bi < 6; ++bi) {
+        const Block bk = blocks[bi];
+        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
+        const uint32_t total = bk.width * cnt;
+        for (uint32_t i = threadIdx.x; i < total; i += kBwdGroup) {
+            const float v = zero ? 0.0f : tile[bk.row + i % bk.width][i / bk.width];
+            dst[i] = add ? dst[i] + v : v;
+        }
+    }
+}
+
 // One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
 // residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of the 59
 // attribute rows in shared memory with bulk copies (as the forward preprocess does): the geometry rows
@@ -256,18 +276,7 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
         }
     }
     __syncthreads();
-    // the CTA's Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute block
-    struct Block { uint32_t row, width, base; };
-    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
-                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
-#pragma unroll
-    for (int bi = 0; bi < 6; ++bi) {
-        const Block bk = blocks[bi];
-        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
-        const uint32_t total = bk.width * cnt;
-        for (uint32_t i = lt; i < total; i += kBwdGroup)
-            dst[i] = any ? s_rows[bk.row + i % bk.width][i / bk.width] : 0.0f;
-    }
+    write_packed(s_rows, out, n, g0, cnt, !any, false);
 }
 
 // Several views of one scene: one thread per Gaussian stages the 59 attribute rows once (bulk copies)
@@ -318,19 +327,7 @@ __global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward_multi(const f
         }
     }
     __syncthreads();
-    struct Block { uint32_t row, width, base; };
-    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
-                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
-#pragma unroll
-    for (int bi = 0; bi < 6; ++bi) {
-        const Block bk = blocks[bi];
-        float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
-        const uint32_t total = bk.width * cnt;
-        for (uint32_t i = lt; i < total; i += kBwdGroup) {
-            const float val = s_grad[bk.row + i % bk.width][i / bk.width];
-            dst[i] = add ? dst[i] + val : val;
-        }
-    }
+    write_packed(s_grad, out, n, g0, cnt, false, add != 0);
 }
 
 }  // namespace

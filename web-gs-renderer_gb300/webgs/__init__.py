@@ -354,8 +354,30 @@ def autotune(packed: np.ndarray, count: int, views: list, iters: int = 5, device
     p = np.ascontiguousarray(packed, dtype=np.float32)
     _check(library().gs_autotune(C.byref(base), _ptr(p), count, arr, len(views), iters, C.byref(best), C.byref(ms)),
            None, "gs_autotune")
-    return {"tile_size": best.tile_size, "digit_bits": best.digit_bits, "raster_batch": best.raster_batch,
-            "sort_block": best.sort_block}, ms.value
+    return _config_dict(best), ms.value
+
+
+def autotune_scenes(scenes: list, views: list, view_scene: list, iters: int = 3, device: int = 0,
+                    max_instance_factor: int = 64) -> tuple[dict, float]:
+    """The same sweep over a whole batch (gs_autotune_scenes): scenes = [(packed, count), ...], view i
+    renders scenes[view_scene[i]]; returns the fastest configuration and its ms per batch."""
+    base = Config()
+    library().gs_config_default(C.byref(base))
+    base.device, base.max_instance_factor = device, max_instance_factor
+    arrays = [np.ascontiguousarray(p, dtype=np.float32) for p, _ in scenes]
+    ptrs = (C.c_void_p * len(arrays))(*[_ptr(a) for a in arrays])
+    counts = (C.c_uint32 * len(scenes))(*[int(c) for _, c in scenes])
+    vs = (C.c_uint32 * len(views))(*[int(i) for i in view_scene])
+    arr = (View * len(views))(*views)
+    best, ms = Config(), C.c_float()
+    _check(library().gs_autotune_scenes(C.byref(base), ptrs, counts, len(scenes), arr, vs, len(views), iters,
+                                        C.byref(best), C.byref(ms)), None, "gs_autotune_scenes")
+    return _config_dict(best), ms.value
+
+
+def _config_dict(cfg: Config) -> dict:
+    return {"tile_size": cfg.tile_size, "digit_bits": cfg.digit_bits, "raster_batch": cfg.raster_batch,
+            "sort_block": cfg.sort_block}
 
 
 # ---- Camera (src/renderer/camera.js) -------------------------------------------------------------

@@ -103,6 +103,8 @@ SIGNATURES = [
                                     C.c_int32]),
     ("gs_autotune", C.c_int, [C.POINTER(Config), C.c_void_p, C.c_uint32, C.POINTER(View), C.c_uint32, C.c_uint32,
                               C.POINTER(Config), C.POINTER(C.c_float)]),
+    ("gs_autotune_scenes", C.c_int, [C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(View),
+                                     C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(Config), C.POINTER(C.c_float)]),
     ("gs_get_debug", C.c_int, [C.c_void_p, C.POINTER(Debug)]),
     ("gs_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
     ("gs_loss_l1_ssim", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
