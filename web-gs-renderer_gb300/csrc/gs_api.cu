@@ -85,7 +85,7 @@ struct Frame {
         ctl.release(); view.release(); rec.release(); meta.release(); counts.release(); offsets.release();
         for (int b = 0; b < 2; ++b) { keys[b].release(); vals[b].release(); }
         flags.release(); ranges.release(); rgba8.release(); n_contrib.release(); rgb.release(); final_t.release();
-        grad2d.release(); dl_stage.release();
+        order.release(); grad2d.release(); dl_stage.release();
         if (h_ctl) cudaFreeHost(h_ctl);
         h_ctl = nullptr;
     }
@@ -214,7 +214,8 @@ int frame_args(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, FrameArg
 int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     const uint32_t radix = 1u << ctx->cfg.digit_bits;
     const void* before[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
-                            f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p};
+                            f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p,
+                            f.order.p};
     GS_CK(f.rec.reserve((size_t)a.n * kRecFloat4));
     GS_CK(f.meta.reserve(a.n));
     GS_CK(f.counts.reserve(((size_t)a.n + 1 + 7) / 8 * 8));
@@ -238,7 +239,8 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     GS_CK(f.final_t.reserve(pix));
     GS_CK(f.n_contrib.reserve(pix));
     const void* after[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
-                           f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p};
+                           f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p,
+                            f.order.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) ++ctx->alloc_gen;
     return GS_OK;
 }
