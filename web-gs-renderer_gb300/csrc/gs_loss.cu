@@ -35,11 +35,20 @@ static_assert(kT * (kT / kRunV) == kThreads, "one vertical run per thread");
 // outside) into dst (pitch kPitchIn).
 __device__ __forceinline__ void stage_channel(const float* __restrict__ img, uint32_t W, uint32_t H, int tx0,
                                               int ty0, int ch, float* dst) {
-    for (int i = threadIdx.x; i < kH * kH; i += kThreads) {
+    // a fixed trip count, so that all of a thread's loads are in flight before the first store
+    constexpr int kIters = (kH * kH + kThreads - 1) / kThreads;
+    float v[kIters];
+#pragma unroll
+    for (int it = 0; it < kIters; ++it) {
+        const int i = threadIdx.x + it * kThreads;
         const int ly = i / kH, lx = i - ly * kH, gx = tx0 + lx, gy = ty0 + ly;
-        float v = 0.0f;
-        if (gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H) v = img[((size_t)gy * W + gx) * 3 + ch];
-        dst[ly * kPitchIn + lx] = v;
+        v[it] = 0.0f;
+        if (i < kH * kH && gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H) v[it] = img[((size_t)gy * W + gx) * 3 + ch];
+    }
+#pragma unroll
+    for (int it = 0; it < kIters; ++it) {
+        const int i = threadIdx.x + it * kThreads;
+        if (i < kH * kH) dst[(i / kH) * kPitchIn + i % kH] = v[it];
     }
 }
 
@@ -113,10 +122,10 @@ __global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__
         const float sxx = m[o][2] - mx * mx, syy = m[o][3] - my * my, sxy = m[o][4] - mx * my;
         const float A1 = 2.0f * mx * my + C1, A2 = 2.0f * sxy + C2;
         const float B1 = mx * mx + my * my + C1, B2 = sxx + syy + C2;
-        const float inv_b = 1.0f / (B1 * B2);
+        const float inv_b = 1.0f / (B1 * B2);  // 1/B1 = B2 inv_b, 1/B2 = B1 inv_b
         const float sv = A1 * A2 * inv_b;
-        const float ds_dmx = (2.0f * my * A2) * inv_b - sv * (2.0f * mx) / B1;
-        const float ds_dsxx = -sv / B2;
+        const float ds_dmx = (2.0f * my * A2) * inv_b - sv * (2.0f * mx) * (B2 * inv_b);
+        const float ds_dsxx = -sv * (B1 * inv_b);
         const float ds_dsxy = 2.0f * A1 * inv_b;
         const size_t po = (size_t)gy * W + gx;
         partial[(ch * 3 + 0) * P + po] = ds_dmx + ds_dsxx * (-2.0f * mx) + ds_dsxy * (-my);
@@ -157,12 +166,25 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
     const int tx0 = blockIdx.x * kT - kR, ty0 = blockIdx.y * kT - kR;
     const int tid = threadIdx.x;
     const size_t P = (size_t)W * H;
-    for (int i = tid; i < kH * kH; i += kThreads) {
-        const int ly = i / kH, lx = i - ly * kH, gx = tx0 + lx, gy = ty0 + ly;
-        const bool in = gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H;
-        const size_t o = in ? (size_t)gy * W + gx : 0;
+    {
+        constexpr int kIters = (kH * kH + kThreads - 1) / kThreads;
+        float v[kIters][3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) sp[q][ly * kPitchIn + lx] = in ? partial[(ch * 3 + q) * P + o] : 0.0f;
+        for (int it = 0; it < kIters; ++it) {
+            const int i = tid + it * kThreads;
+            const int ly = i / kH, lx = i - ly * kH, gx = tx0 + lx, gy = ty0 + ly;
+            const bool in = i < kH * kH && gx >= 0 && gx < (int)W && gy >= 0 && gy < (int)H;
+            const size_t o = in ? (size_t)gy * W + gx : 0;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) v[it][q] = in ? partial[(ch * 3 + q) * P + o] : 0.0f;
+        }
+#pragma unroll
+        for (int it = 0; it < kIters; ++it) {
+            const int i = tid + it * kThreads;
+            if (i < kH * kH)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) sp[q][(i / kH) * kPitchIn + i % kH] = v[it][q];
+        }
     }
     __syncthreads();
     if (tid < kItemsH) {
