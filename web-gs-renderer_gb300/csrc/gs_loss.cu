@@ -70,27 +70,28 @@ __global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__
     __syncthreads();
     if (tid < kItemsH) {
         const int r = tid / (kT / kRunH), c0 = (tid % (kT / kRunH)) * kRunH;
-        float a[kRunH + 2 * kR], b[kRunH + 2 * kR];
+        constexpr int kIn = kRunH + 2 * kR;
+        float a[kIn], b[kIn];
 #pragma unroll
-        for (int j = 0; j < kRunH + 2 * kR; ++j) {
+        for (int j = 0; j < kIn; ++j) {
             a[j] = sx[r * kPitchIn + c0 + j];
             b[j] = sy[r * kPitchIn + c0 + j];
         }
+        // one quantity at a time (x, y, x^2, y^2, xy): its inputs formed once, then one fused
+        // multiply-add per tap and output
 #pragma unroll
-        for (int o = 0; o < kRunH; ++o) {
-            float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+        for (int qn = 0; qn < 5; ++qn) {
+            float v[kIn];
 #pragma unroll
-            for (int k = 0; k < 2 * kR + 1; ++k) {
-                const float av = a[o + k], bv = b[o + k], w = win.w[k];
-                const float wa = w * av, wb = w * bv;
-                s0 += wa;
-                s1 += wb;
-                s2 = fmaf(wa, av, s2);
-                s3 = fmaf(wb, bv, s3);
-                s4 = fmaf(wa, bv, s4);
+            for (int j = 0; j < kIn; ++j)
+                v[j] = qn == 0 ? a[j] : qn == 1 ? b[j] : qn == 2 ? a[j] * a[j] : qn == 3 ? b[j] * b[j] : a[j] * b[j];
+#pragma unroll
+            for (int o = 0; o < kRunH; ++o) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 2 * kR + 1; ++k) acc = fmaf(win.w[k], v[o + k], acc);
+                hm[qn][r * kPitchH + c0 + o] = acc;
             }
-            const int q = r * kPitchH + c0 + o;
-            hm[0][q] = s0; hm[1][q] = s1; hm[2][q] = s2; hm[3][q] = s3; hm[4][q] = s4;
         }
     }
     __syncthreads();
@@ -166,6 +167,18 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
     const int tx0 = blockIdx.x * kT - kR, ty0 = blockIdx.y * kT - kR;
     const int tid = threadIdx.x;
     const size_t P = (size_t)W * H;
+    const int c = tid % kT, r0 = (tid / kT) * kRunV;
+    const int gx = blockIdx.x * kT + c;
+    // this thread's x and y, loaded first so that they arrive during the staging and the filtering
+    float xv[kRunV], yv[kRunV];
+#pragma unroll
+    for (int o = 0; o < kRunV; ++o) {
+        const int gy = blockIdx.y * kT + r0 + o;
+        const bool in = gx < (int)W && gy < (int)H;
+        const size_t q = in ? ((size_t)gy * W + gx) * 3 + ch : 0;
+        xv[o] = in ? x[q] : 0.0f;
+        yv[o] = in ? y[q] : 0.0f;
+    }
     {
         constexpr int kIters = (kH * kH + kThreads - 1) / kThreads;
         float v[kIters][3];
@@ -204,8 +217,6 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
         }
     }
     __syncthreads();
-    const int c = tid % kT, r0 = (tid / kT) * kRunV;
-    const int gx = blockIdx.x * kT + c;
     float bl[kRunV][3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -226,9 +237,9 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
         const int gy = blockIdx.y * kT + r0 + o;
         if (gx >= (int)W || gy >= (int)H) continue;
         const size_t q = ((size_t)gy * W + gx) * 3 + ch;
-        const float xv = x[q], yv = y[q], d = xv - yv;
+        const float d = xv[o] - yv[o];
         const float g_l1 = (d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f));
-        dl[q] = g_l1 - lambda * inv * (bl[o][0] + 2.0f * xv * bl[o][1] + yv * bl[o][2]);
+        dl[q] = g_l1 - lambda * inv * (bl[o][0] + 2.0f * xv[o] * bl[o][1] + yv[o] * bl[o][2]);
     }
 }
 
