@@ -52,12 +52,12 @@ __device__ __forceinline__ float warp_reduce_scatter8(const float v[8]) {
 }
 
 // One pixel's backward state: its last contributor L (1-based position in the tile range), the
-// transmittance in front of the splat being visited, its colour gradient, and the colour blended
-// behind that splat (acc) with the previously visited splat's alpha and colour.
+// transmittance in front of the splat being visited, its colour gradient, and the colour the splats
+// behind the visited one added to the pixel (S = sum over them of alpha_j T_j c_j).
 struct PixState {
     uint32_t L;
     float fx, fy, T, dr, dg, db;
-    float acc_r, acc_g, acc_b, last_a, last_r, last_g, last_b;
+    float s_r, s_g, s_b;
 };
 
 __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, uint32_t width, uint32_t height,
@@ -68,7 +68,7 @@ __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, ui
     p.L = 0;
     p.T = 1.0f;
     p.dr = p.dg = p.db = 0.0f;
-    p.acc_r = p.acc_g = p.acc_b = p.last_a = p.last_r = p.last_g = p.last_b = 0.0f;
+    p.s_r = p.s_g = p.s_b = 0.0f;
     if (x < width && y < height) {
         const size_t q = (size_t)y * width + x;
         p.L = n_contrib[q];
@@ -82,7 +82,9 @@ __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, ui
 // Visits the splat at 1-based range position pos for one pixel: the same power / exp / alpha
 // decisions as the forward (bit for bit), then adds this pixel's share of the splat's gradients to
 // g = {d px, d py, d conic.x, d conic.y, d conic.z, d opacity, d r, d g, d b}. T is recovered by
-// division; the approximate divide (2 ulp, denominator >= 0.01) is accurate enough for a gradient.
+// division (the approximate reciprocal, 2 ulp, of 1 - alpha >= 0.01 is accurate enough for a
+// gradient). With C = sum_i alpha_i T_i c_i and T_{i+1} = T_i (1 - alpha_i),
+// dC/dalpha_i = T_i c_i - S_i / (1 - alpha_i), S_i being the colour added behind splat i.
 __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4& a, const float4& b,
                                          const float2& c, float g[9]) {
     if (pos > p.L) return false;
@@ -95,17 +97,16 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
     if (!(alpha >= kEpsilon)) return false;
     // from here on only gradients are formed: fused multiply-adds are fine (the decisions above
     // follow the forward's pinned arithmetic)
-    const float Tb = __fdividef(p.T, 1.0f - alpha);  // transmittance in front of this splat
-    const float keep = 1.0f - p.last_a;
-    p.acc_r = __fmaf_rn(p.last_a, p.last_r, keep * p.acc_r);
-    p.acc_g = __fmaf_rn(p.last_a, p.last_g, keep * p.acc_g);
-    p.acc_b = __fmaf_rn(p.last_a, p.last_b, keep * p.acc_b);
+    const float ria = __fdividef(1.0f, 1.0f - alpha);
+    const float Tb = p.T * ria;  // transmittance in front of this splat
     const float w = alpha * Tb;
     g[6] = __fmaf_rn(w, p.dr, g[6]);
     g[7] = __fmaf_rn(w, p.dg, g[7]);
     g[8] = __fmaf_rn(w, p.db, g[8]);
-    const float dalpha =
-        Tb * __fmaf_rn(b.z - p.acc_r, p.dr, __fmaf_rn(b.w - p.acc_g, p.dg, (c.x - p.acc_b) * p.db));
+    const float ur = __fmaf_rn(Tb, b.z, -(p.s_r * ria));
+    const float ug = __fmaf_rn(Tb, b.w, -(p.s_g * ria));
+    const float ub = __fmaf_rn(Tb, c.x, -(p.s_b * ria));
+    const float dalpha = __fmaf_rn(ur, p.dr, __fmaf_rn(ug, p.dg, ub * p.db));
     if (og <= kAlphaClamp) {
         const float gp = dalpha * og;  // dL/dpower
         const float gh = -0.5f * gp;
@@ -116,10 +117,9 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
         g[4] = __fmaf_rn(gh * dy, dy, g[4]);
         g[5] = __fmaf_rn(dalpha, G, g[5]);
     }
-    p.last_a = alpha;
-    p.last_r = b.z;
-    p.last_g = b.w;
-    p.last_b = c.x;
+    p.s_r = __fmaf_rn(w, b.z, p.s_r);
+    p.s_g = __fmaf_rn(w, b.w, p.s_g);
+    p.s_b = __fmaf_rn(w, c.x, p.s_b);
     p.T = Tb;
     return true;
 }
