@@ -81,7 +81,8 @@ __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, ui
 
 // Visits the splat at 1-based range position pos for one pixel: the same power / exp / alpha
 // decisions as the forward (bit for bit), then adds this pixel's share of the splat's gradients to
-// g = {d px, d py, d conic.x, d conic.y, d conic.z, d opacity, d r, d g, d b}. T is recovered by
+// g = {d px, d py, d conic.x, d conic.y, d conic.z, d opacity, d r, d g, d b}, the first five without
+// their constant factors (-1, -1, -1/2, -1, -1/2, applied after the warp reduction). T is recovered by
 // division (the approximate reciprocal, 2 ulp, of 1 - alpha >= 0.01 is accurate enough for a
 // gradient). With C = sum_i alpha_i T_i c_i and T_{i+1} = T_i (1 - alpha_i),
 // dC/dalpha_i = T_i c_i - S_i / (1 - alpha_i), S_i being the colour added behind splat i.
@@ -108,13 +109,15 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
     const float ub = __fmaf_rn(Tb, c.x, -(p.s_b * ria));
     const float dalpha = __fmaf_rn(ur, p.dr, __fmaf_rn(ug, p.dg, ub * p.db));
     if (og <= kAlphaClamp) {
+        // the constant factors of d power / d(px, py, conic) (-1, -1, -1/2, -1, -1/2) are applied
+        // once per splat after the warp reduction (kGradSign)
         const float gp = dalpha * og;  // dL/dpower
-        const float gh = -0.5f * gp;
-        g[0] = __fmaf_rn(gp, __fmaf_rn(-a.z, dx, -(a.w * dy)), g[0]);
-        g[1] = __fmaf_rn(gp, __fmaf_rn(-b.x, dy, -(a.w * dx)), g[1]);
-        g[2] = __fmaf_rn(gh * dx, dx, g[2]);
-        g[3] = __fmaf_rn(-gp * dx, dy, g[3]);
-        g[4] = __fmaf_rn(gh * dy, dy, g[4]);
+        const float gpdx = gp * dx, gpdy = gp * dy;
+        g[0] = __fmaf_rn(gp, __fmaf_rn(a.z, dx, a.w * dy), g[0]);
+        g[1] = __fmaf_rn(gp, __fmaf_rn(b.x, dy, a.w * dx), g[1]);
+        g[2] = __fmaf_rn(gpdx, dx, g[2]);
+        g[3] = __fmaf_rn(gpdx, dy, g[3]);
+        g[4] = __fmaf_rn(gpdy, dy, g[4]);
         g[5] = __fmaf_rn(dalpha, G, g[5]);
     }
     p.s_r = __fmaf_rn(w, b.z, p.s_r);
@@ -162,6 +165,9 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
     const float tx0 = (float)(tx * TILE), tx1 = (float)(tx * TILE + TILE - 1u);
     const float ty0 = (float)(ty * TILE), ty1 = (float)(ty * TILE + TILE - 1u);
 
+    // factor of the value this lane ends up holding after warp_reduce_scatter8 (see pix_step)
+    const float kGradSign[8] = {-1.0f, -1.0f, -0.5f, -1.0f, -0.5f, 1.0f, 1.0f, 1.0f};
+    const float sign = kGradSign[(lane >> 2) & 7u];
     PixState p0, p1;
     pix_load(p0, x, y, width, height, final_t, n_contrib, dl_drgb);
     pix_load(p1, x, y + 4u, width, height, final_t, n_contrib, dl_drgb);
@@ -216,7 +222,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                     const bool c0 = pix_step(p0, pos, a, b, c, g);
                     const bool c1 = pix_step(p1, pos, a, b, c, g);
                     if (__any_sync(0xffffffffu, c0 || c1)) {
-                        const float mine = warp_reduce_scatter8(g);  // total of value (lane >> 2) & 7
+                        const float mine = sign * warp_reduce_scatter8(g);  // total of value (lane >> 2) & 7
                         const float blue = warp_sum(g[8]);
                         const uint32_t gi = s_g[j];
                         if (gi < n) {
