@@ -836,7 +836,7 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 // Raster backward of frame f into f.grad2d (dL/d of its per-Gaussian 2D quantities).
 static int enqueue_raster_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, cudaStream_t s,
                                    cudaEvent_t* ev = nullptr) {
-    GS_CK(f.grad2d.reserve((size_t)scene->n * 9));
+    GS_CK(f.grad2d.reserve((size_t)scene->n * 9 + 4));  // + 4: the preprocess backward copies whole 16-byte units
     if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
     if (ev) cudaEventRecord(ev[0], s);
     launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[f.sorted_buf].p, f.rec.p,

@@ -216,31 +216,37 @@ __device__ __forceinline__ void write_packed(const float (*tile)[kBwdPitch], flo
 }
 
 // One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
-// residency). A CTA with at least one visible Gaussian stages its 128-Gaussian slice of the 59
-// attribute rows in shared memory with bulk copies (as the forward preprocess does): the geometry rows
-// on one mbarrier and the 45 f_rest rows on another, so the geometric part of the chain rule overlaps
-// the arrival of the SH coefficients. The gradients replace the staged attributes in shared memory
-// and the CTA writes its slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest
-// blocks, the layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros.
+// residency). Everything a CTA reads comes in by bulk copies into shared memory, in two steps so that
+// only one memory round trip precedes any arithmetic: first the view block, the slice's tilesTouched
+// counts and 2D gradients and its 14 geometry attribute rows (one mbarrier); then, if any Gaussian of
+// the slice is visible, its 45 f_rest rows (a second mbarrier), whose arrival overlaps the geometric
+// part of the chain rule. The gradients replace the staged attributes in shared memory and the CTA
+// writes its slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest blocks, the
+// layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros.
+// Reads past the slice: counts are read in whole 16-byte units (the buffer holds roundup(N + 1, 8)
+// entries) and grad2d likewise (it holds 9N + 4 floats).
 __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
                                                                    uint32_t n, const ViewBlock* __restrict__ vb,
                                                                    const uint32_t* __restrict__ counts,
                                                                    const float* __restrict__ grad2d,
                                                                    float* __restrict__ out, uint32_t* status) {
+    static_assert(sizeof(ViewBlock) % 16 == 0, "the view block is copied in 16-byte units");
     __shared__ __align__(128) float s_rows[kRows][kBwdPitch];
-    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
-    __shared__ ViewBlock sv;
+    __shared__ __align__(16) float s_d2[kBwdGroup * 9];
+    __shared__ __align__(16) uint32_t s_cnt[kBwdGroup];
+    __shared__ __align__(16) ViewBlock sv;
+    __shared__ __align__(8) uint64_t s_bar[2];  // [0]: view, counts, 2D gradients, geometry rows; [1]: f_rest rows
     const uint32_t lt = threadIdx.x;
     const uint32_t g0 = blockIdx.x * kBwdGroup;
-    const uint32_t g = g0 + lt;
     const uint32_t cnt = min(kBwdGroup, n - g0);  // Gaussians of this CTA (g0 < n)
-    const bool vis = g < n && counts[g] != 0u;
+    // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and spans a
+    // multiple of 256 bytes (g0 < n <= stride)
+    const uint32_t cols = min(kBwdGroup, stride - g0);
     if (lt == 0) {
         mbar_init(&s_bar[0], 1);
         mbar_init(&s_bar[1], 1);
     }
-    if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(vb)[lt];
-    const int any = __syncthreads_or(vis);
+    __syncthreads();
     // bounded wait: on expiry the timeout is recorded and the kernel goes on with what is there
     auto wait_bar = [&](uint64_t* bar) {
         uint32_t spins = 0;
@@ -251,23 +257,29 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
             }
         }
     };
+    if (lt == 0) {
+        const uint32_t cnt_bytes = ((cnt + 3u) & ~3u) * 4u;
+        const uint32_t d2_bytes = (cnt * 36u + 15u) & ~15u;
+        mbar_expect_tx(&s_bar[0], (uint32_t)sizeof(ViewBlock) + cnt_bytes + d2_bytes + kRowRest * cols * 4u);
+        bulk_g2s(&sv, vb, (uint32_t)sizeof(ViewBlock), &s_bar[0]);
+        bulk_g2s(s_cnt, counts + g0, cnt_bytes, &s_bar[0]);
+        bulk_g2s(s_d2, grad2d + (size_t)9 * g0, d2_bytes, &s_bar[0]);
+        for (int r = 0; r < kRowRest; ++r)
+            bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
+    }
+    wait_bar(&s_bar[0]);
+    const bool vis = lt < cnt && s_cnt[lt] != 0u;
+    const int any = __syncthreads_or(vis);
     if (any) {
         if (lt == 0) {
-            // stride and g0 are multiples of 64 floats: every row slice starts 256-byte aligned and
-            // spans a multiple of 256 bytes (g0 < n <= stride)
-            const uint32_t cols = min(kBwdGroup, stride - g0);
-            mbar_expect_tx(&s_bar[0], kRowRest * cols * 4u);
-            for (int r = 0; r < kRowRest; ++r)
-                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
             mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
             for (int r = kRowRest; r < kRows; ++r)
                 bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
         }
-        wait_bar(&s_bar[0]);
         if (vis) {
             auto R_ = [&](int row) { return s_rows[row][lt]; };
             auto W_ = [&](int row, float v) { s_rows[row][lt] = v; };
-            backward_gaussian(sv, grad2d + (size_t)9 * g, R_, W_, [&]() { wait_bar(&s_bar[1]); });
+            backward_gaussian(sv, s_d2 + 9 * lt, R_, W_, [&]() { wait_bar(&s_bar[1]); });
         } else {
             // every thread waits for the f_rest copies before it overwrites its column or leaves: no
             // bulk copy may still write into shared memory that is reused or released
