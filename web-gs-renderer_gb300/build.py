@@ -31,13 +31,13 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
 # Translation units whose results are not bit-pinned (gradients, the loss) may contract a*b+c into
-# fused multiply-adds.
+# fused multiply-adds and use the approximate division and square root (denormals are kept).
 CONTRACTED = {"gs_preprocess_backward.cu", "gs_loss.cu"}
 
 
 def _nvcc_flags(src: Path) -> list[str]:
     if src.name in CONTRACTED:
-        return [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS]
+        return [{"-fmad=false": "-fmad=true", "-prec-div=true": "-prec-div=false", "-prec-sqrt=true": "-prec-sqrt=false"}.get(f, f) for f in NVCC_FLAGS]
     return NVCC_FLAGS
 
 

@@ -8,7 +8,7 @@
 //   k_ssim_fwd  moments -> SSIM map -> its three partials (to global) + per-block SSIM and L1 sums;
 //   k_ssim_bwd  blurred partials + the L1 term -> dL/dx.
 // Images are H x W x 3 (pixel-interleaved). The loss is not bit-pinned: this file is built with
-// multiply-add contraction and its filters use fused multiply-adds.
+// multiply-add contraction and the approximate division, and its filters use fused multiply-adds.
 #include <cmath>
 
 #include "gs_kernels.h"

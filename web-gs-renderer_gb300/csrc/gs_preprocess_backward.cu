@@ -2,8 +2,9 @@
 // gradients the raster backward accumulates (dL/d pixel position, conic, opacity, colour) to the 59
 // packed attributes, for one view or for several views of one scene.
 //
-// This file is built with multiply-add contraction: it only forms gradients, and no bit of its output
-// has to match the forward's pinned arithmetic.
+// This file is built with multiply-add contraction and the approximate division and square root, and
+// it recomputes exp with the hardware approximation (__expf): it only forms gradients, and no bit of
+// its output has to match the forward's pinned arithmetic.
 #include "gs_kernels.h"
 
 namespace gs {
@@ -31,7 +32,7 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
     const float wden = clip[3] + kSmallValue;
     // rotation and scale
     float s[3];
-    for (int i = 0; i < 3; ++i) s[i] = pinned_expf(R_(kRowScale + i));
+    for (int i = 0; i < 3; ++i) s[i] = __expf(R_(kRowScale + i));
     const float qr[4] = {R_(kRowQuat + 1), R_(kRowQuat + 2), R_(kRowQuat + 3), R_(kRowQuat + 0)};  // (x, y, z, w)
     const float qlen = sqrtf(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
     const float q[4] = {qr[0] / qlen, qr[1] / qlen, qr[2] / qlen, qr[3] / qlen};
@@ -163,7 +164,7 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
     gp[2] += (gdz - dz_ * ddot) / vlen;
     for (int i = 0; i < 3; ++i) W_(kRowPos + i, gp[i]);
     // opacity logit
-    const float op = 1.0f / (1.0f + pinned_expf(-R_(kRowOpacity)));
+    const float op = 1.0f / (1.0f + __expf(-R_(kRowOpacity)));
     W_(kRowOpacity, go * op * (1.0f - op));
     // Sigma = A A^T -> A -> (R, s) -> (quaternion, log-scale)
     float gAm[3][3];
