@@ -291,7 +291,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     FrameCtl* ctl = f.ctl.p;
     if (profile) cudaEventRecord(ctx->ev[0], s);
     if (!preprocessed) {
-        launch_frame_begin(ctl, s);
+        launch_frame_begin(ctl, s, f.ranges.p, a.tiles_x * a.tiles_y * 2u);
         launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p,
                           f.counts.p, ctl, s);
     }
@@ -307,7 +307,6 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
         cur ^= 1;
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
-    cudaMemsetAsync(f.ranges.p, 0, (size_t)a.tiles_x * a.tiles_y * 2 * sizeof(uint32_t), s);
     launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, a.max_instance, 0, s);
     launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order.p, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
@@ -373,7 +372,7 @@ int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, con
                     for (uint32_t v = 0; v < mv.count; ++v) {
                         const size_t j = group[c0 + v];
                         Frame& f = *frames[j];
-                        launch_frame_begin(f.ctl.p, ctx->stream);
+                        launch_frame_begin(f.ctl.p, ctx->stream, f.ranges.p, args[j].tiles_x * args[j].tiles_y * 2u);
                         mv.view[v] = args[j].view;
                         mv.rec[v] = f.rec.p;
                         mv.meta[v] = f.meta.p;

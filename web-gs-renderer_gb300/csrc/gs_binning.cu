@@ -68,8 +68,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
     return r;
 }
 
-__global__ void k_frame_begin(FrameCtl* ctl) {
+__global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words) {
+    pdl_wait();
     const uint32_t t = threadIdx.x;
+    for (uint32_t i = t; i < range_words; i += blockDim.x) ranges[i] = 0u;  // ranges cleared (renderer.js:919)
     if (t == 0) {
         ctl->seq = (ctl->seq & ~15u) + 16u;
         ctl->status = 0u;
@@ -101,6 +103,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
                                                             uint32_t* __restrict__ offsets, uint32_t* __restrict__ keys,
                                                             uint32_t* __restrict__ vals, FrameCtl* ctl,
                                                             uint64_t* flags, uint32_t slot) {
+    pdl_wait();
     __shared__ uint32_t s_off[kScanPartition + 1];
     __shared__ uint2 s_meta[kScanPartition];  // (minX | minY << 16, rect width | depth16 << 16)
     __shared__ uint32_t s_own[kScanPartition];  // owner (local Gaussian) of each slot of an emit chunk
@@ -354,6 +357,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                                                            const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
                                                            uint32_t dmask, const uint32_t* __restrict__ hist,
                                                            FrameCtl* ctl, uint64_t* flags, uint32_t slot) {
+    pdl_wait();
     constexpr uint32_t RADIX = 1u << BITS;
     const uint32_t MASK = dmask & (RADIX - 1u);  // digit mask of this pass (narrower on a last partial digit)
     constexpr uint32_t WARPS = kSortThreads / 32;
@@ -506,6 +510,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
 // timed-out sort; they are skipped.
 __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCtl* ctl, uint32_t tiles,
                               uint32_t* __restrict__ ranges) {
+    pdl_wait();
     const uint32_t n = ctl->sorted_count;
     const uint32_t quads = (n + 3u) / 4u;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += gridDim.x * blockDim.x) {
@@ -556,6 +561,7 @@ constexpr uint32_t kOrderPer = 8;  // tiles per thread per round (8192 tiles per
 
 __global__ void __launch_bounds__(1024) k_tile_order(const uint32_t* __restrict__ ranges, uint32_t tiles,
                                                      uint32_t* __restrict__ order) {
+    pdl_wait();
     __shared__ uint32_t s_bin[64];
     const uint32_t tid = threadIdx.x;
     if (tid < 64u) s_bin[tid] = 0u;
@@ -616,14 +622,16 @@ int sm_count() {
 
 }  // namespace
 
-void launch_frame_begin(FrameCtl* ctl, cudaStream_t s) { k_frame_begin<<<1, 256, 0, s>>>(ctl); }
+void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges, uint32_t range_words) {
+    launch_pdl(k_frame_begin, dim3(1), dim3(1024), s, ctl, ranges, range_words);
+}
 
 void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uint32_t tiles_x, uint32_t max_instance,
                       uint32_t digit_bits, uint32_t passes, uint32_t* offsets, uint32_t* keys, uint32_t* vals,
                       FrameCtl* ctl, uint64_t* flags, uint32_t slot, cudaStream_t s) {
     const uint32_t parts = (n + 1u + kScanPartition - 1u) / kScanPartition;
-    k_scan_emit<<<parts, kScanThreads, 0, s>>>(counts, meta, n, tiles_x, max_instance, digit_bits, passes, offsets,
-                                               keys, vals, ctl, flags, slot);
+    launch_pdl(k_scan_emit, dim3(parts), dim3(kScanThreads), s, counts, meta, n, tiles_x, max_instance, digit_bits,
+               passes, offsets, keys, vals, ctl, flags, slot);
 }
 
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
@@ -660,8 +668,8 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
     if (parts > cap) parts = cap;
     if (parts == 0) parts = 1;
 #define GS_ONESWEEP(B, I)                                                                                      \
-    k_onesweep<B, I><<<parts, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n_dev, n_host, shift, \
-                                                    dmask, hist, ctl, flags, slot)
+    launch_pdl(k_onesweep<B, I>, dim3(parts), dim3(kSortThreads), s, keys_in, vals_in, keys_out, vals_out, n_dev, \
+               n_host, shift, dmask, hist, ctl, flags, slot)
     if (digit_bits == 4) {
         if (small) GS_ONESWEEP(4, 8); else GS_ONESWEEP(4, 16);
     } else {
@@ -671,7 +679,7 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
 }
 
 void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* order, cudaStream_t s) {
-    k_tile_order<<<1, 1024, 0, s>>>(ranges, tiles, order);
+    launch_pdl(k_tile_order, dim3(1), dim3(1024), s, ranges, tiles, order);
 }
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
@@ -681,7 +689,7 @@ void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tile
     const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 16u;
     if (grid > cap) grid = cap;
     if (grid == 0) grid = 1;
-    k_tile_ranges<<<grid, 256, 0, s>>>(keys, ctl, tiles, ranges);
+    launch_pdl(k_tile_ranges, dim3(grid), dim3(256), s, keys, ctl, tiles, ranges);
 }
 
 }  // namespace gs

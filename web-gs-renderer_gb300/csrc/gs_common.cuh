@@ -154,6 +154,13 @@ __device__ __forceinline__ uint32_t warp_lookback(const uint64_t* words, uint32_
 }
 
 // ---- bulk-copy (TMA) staging helpers ------------------------------------------------------------
+// Programmatic dependent launch (griddepcontrol): a kernel launched with launch_pdl calls pdl_wait()
+// before touching anything; it returns once the kernel before it on the stream has completed and its
+// writes are visible (at once for a kernel launched without the attribute). No kernel triggers its
+// dependents early: an explicit trigger at the top of every kernel measured slower in the frame's graph
+// (its dependents' CTAs sat in the wait), while the implicit trigger as CTAs exit keeps the gain.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");

@@ -1,6 +1,7 @@
 // gs_kernels.h -- launch wrappers of the splat kernels (host side), used by the C ABI in gs_api.cu.
 #pragma once
 #include <cstdint>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "gs_common.cuh"
@@ -18,8 +19,28 @@ constexpr int kRecFloat4 = 3;
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s);
 // rows -> packed (used for gradients).
 
+// Launches kernel k on stream s as a programmatic dependent of the kernel before it on s: k's launch
+// is set up while that kernel runs and its CTAs start as that kernel's CTAs exit, instead of after the
+// whole grid has drained (inside a captured graph the edge stays programmatic). k must call pdl_wait()
+// before anything else.
+template <typename... Params, typename... Args>
+inline void launch_pdl(void (*k)(Params...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 // ---- frame ----------------------------------------------------------------------------------
-void launch_frame_begin(FrameCtl* ctl, cudaStream_t s);
+// Resets the frame control block and, when given, clears the frame's tile ranges (range_words words).
+void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges = nullptr, uint32_t range_words = 0);
 
 // Up to kMaxMultiViews views of one scene for launch_preprocess_multi: each view's block and frame
 // outputs.

@@ -263,6 +263,7 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess(const float* __restric
                                                           const ViewBlock* __restrict__ vb, uint32_t tile,
                                                           float4* __restrict__ rec, uint4* __restrict__ meta,
                                                           uint32_t* __restrict__ counts, FrameCtl* ctl) {
+    pdl_wait();
     __shared__ __align__(128) float s_rows[kRows][kPreGroup];
     __shared__ __align__(8) uint64_t s_bar[2];  // [0]: geometry rows, [1]: f_rest rows
     __shared__ ViewBlock sv;
@@ -384,7 +385,8 @@ __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32
 void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
                        float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s) {
     const uint32_t blocks = (n + kPreGroup - 1u) / kPreGroup;
-    k_preprocess<<<blocks > 0 ? blocks : 1u, kPreGroup, 0, s>>>(rows, stride, n, view, tile, rec, meta, counts, ctl);
+    launch_pdl(k_preprocess, dim3(blocks > 0 ? blocks : 1u), dim3(kPreGroup), s, rows, stride, n, view, tile, rec, meta,
+               counts, ctl);
 }
 
 void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uint32_t tile, const MultiViewFrames& mv,

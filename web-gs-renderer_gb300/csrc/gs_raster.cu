@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
                                                         const FrameCtl* __restrict__ ctl, uint32_t width,
                                                         uint32_t height, uint32_t tiles_x, RasterOut out,
                                                         const uint32_t* __restrict__ order) {
+    pdl_wait();
     constexpr int THREADS = TILE * TILE;
     constexpr int WX = TILE / 8;  // warps across the tile
     __shared__ float4 s_a[BATCH];    // (x, y, conic.x, conic.y)
@@ -147,10 +148,10 @@ void launch_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, c
     const uint32_t grid = tiles_x * tiles_y;
     constexpr int threads = TILE * TILE;
     switch (batch) {
-        case 32: k_raster<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        case 64: k_raster<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        case 128: k_raster<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        default: k_raster<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 32: launch_pdl(k_raster<TILE, 32>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 64: launch_pdl(k_raster<TILE, 64>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 128: launch_pdl(k_raster<TILE, 128>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        default: launch_pdl(k_raster<TILE, 256>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
     }
 }
 
