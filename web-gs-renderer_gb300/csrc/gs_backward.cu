@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                                                                      const float* __restrict__ dl_drgb,
                                                                      float* __restrict__ grad2d,
                                                                      const uint32_t* __restrict__ order) {
+    pdl_wait();
     constexpr int WX = TILE / 8;
     constexpr int kThreads = TILE * TILE / 2;
     __shared__ float4 s_a[BATCH];
@@ -246,10 +247,10 @@ void launch_bwd_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* val
     const uint32_t grid = tiles_x * tiles_y;
     constexpr int threads = TILE * TILE / 2;
     switch (batch) {
-        case 32: k_raster_backward<TILE, 32><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
-        case 64: k_raster_backward<TILE, 64><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
-        case 128: k_raster_backward<TILE, 128><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
-        default: k_raster_backward<TILE, 256><<<grid, threads, 0, s>>>(ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        case 32: launch_pdl(k_raster_backward<TILE, 32>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        case 64: launch_pdl(k_raster_backward<TILE, 64>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        case 128: launch_pdl(k_raster_backward<TILE, 128>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
+        default: launch_pdl(k_raster_backward<TILE, 256>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, final_t, n_contrib, dl, grad2d, order); break;
     }
 }
 

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__
                                                        uint32_t W, uint32_t H, Window win,
                                                        float* __restrict__ partial /* 9 planes */,
                                                        double* __restrict__ block_sums) {
+    pdl_wait();
     __shared__ float sx[kH * kPitchIn], sy[kH * kPitchIn];
     __shared__ float hm[5][kH * kPitchH];
     __shared__ float red[2][kThreads / 32];
@@ -161,6 +162,7 @@ __global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__
 __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__ partial, const float* __restrict__ x,
                                                        const float* __restrict__ y, uint32_t W, uint32_t H,
                                                        Window win, float lambda, float* __restrict__ dl) {
+    pdl_wait();
     __shared__ float sp[3][kH * kPitchIn];
     __shared__ float hp[3][kH * kPitchH];
     const int ch = blockIdx.z;
@@ -245,6 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
 
 // sums[0..1] = column sums of the per-block partials that follow them
 __global__ void k_reduce_sums(double* __restrict__ sums, size_t blocks) {
+    pdl_wait();
     __shared__ double red[2][32];
     double a = 0.0, b = 0.0;
     const double* part = sums + 2;
@@ -302,9 +305,9 @@ void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_
                          float* scratch, double* sums, float* dl, cudaStream_t s) {
     const Window win = make_window();
     const dim3 grid = loss_grid(width, height), block(kThreads);
-    k_ssim_fwd<<<grid, block, 0, s>>>(x, y, width, height, win, scratch, sums + 2);
-    k_reduce_sums<<<1, 1024, 0, s>>>(sums, (size_t)grid.x * grid.y * grid.z);
-    if (dl) k_ssim_bwd<<<grid, block, 0, s>>>(scratch, x, y, width, height, win, lambda, dl);
+    launch_pdl(k_ssim_fwd, grid, block, s, x, y, width, height, win, scratch, sums + 2);
+    launch_pdl(k_reduce_sums, dim3(1), dim3(1024), s, sums, (size_t)grid.x * grid.y * grid.z);
+    if (dl) launch_pdl(k_ssim_bwd, grid, block, s, scratch, x, y, width, height, win, lambda, dl);
 }
 
 }  // namespace gs

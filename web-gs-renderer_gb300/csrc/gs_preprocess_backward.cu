@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
                                                                    const uint32_t* __restrict__ counts,
                                                                    const float* __restrict__ grad2d,
                                                                    float* __restrict__ out, uint32_t* status) {
+    pdl_wait();
     static_assert(sizeof(ViewBlock) % 16 == 0, "the view block is copied in 16-byte units");
     __shared__ __align__(128) float s_rows[kRows][kBwdPitch];
     __shared__ __align__(16) float s_d2[kBwdGroup * 9];
@@ -363,8 +364,8 @@ void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, 
                                 const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
                                 cudaStream_t s) {
     if (n == 0) return;
-    k_preprocess_backward<<<(n + kBwdGroup - 1u) / kBwdGroup, kBwdGroup, 0, s>>>(rows, stride, n, view, counts,
-                                                                                grad2d, out, status);
+    launch_pdl(k_preprocess_backward, dim3((n + kBwdGroup - 1u) / kBwdGroup), dim3(kBwdGroup), s, rows, stride, n, view,
+               counts, grad2d, out, status);
 }
 
 }  // namespace gs
