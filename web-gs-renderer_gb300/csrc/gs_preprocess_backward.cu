@@ -199,19 +199,41 @@ __device__ __forceinline__ void backward_gaussian(const ViewBlock& sv, const flo
 // Writes the CTA's gradient tile (one column per Gaussian, rows as the scene layout) to its slice of
 // the packed layout: the Gaussians [g0, g0 + cnt) occupy one contiguous range of each attribute
 // block, so every block is one coalesced run. zero: write zeros; add: add to what `out` holds.
+// The narrow blocks (1 to 4 values per Gaussian) walk the run one element per lane. The 45-value
+// f_rest block maps lanes to attribute rows instead: a lane reads four consecutive Gaussians of its
+// row with one 16-byte load (eight lanes of a phase hit eight distinct 4-bank groups: no conflict,
+// where a column read down the rows is 4-way) and makes four stores, each of which the warp's 32
+// lanes (32 consecutive rows) complete as one contiguous 128-byte run.
 __device__ __forceinline__ void write_packed(const float (*tile)[kBwdPitch], float* __restrict__ out, uint32_t n,
                                              uint32_t g0, uint32_t cnt, bool zero, bool add) {
     struct Block { uint32_t row, width, base; };
-    const Block blocks[6] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6},
-                             {kRowDc, 3, 10}, {kRowOpacity, 1, 13}, {kRowRest, 45, 14}};
+    const Block blocks[5] = {{kRowPos, 3, 0}, {kRowScale, 3, 3}, {kRowQuat, 4, 6}, {kRowDc, 3, 10}, {kRowOpacity, 1, 13}};
 #pragma unroll
-    for (int bi = 0; bi < 6; ++bi) {
+    for (int bi = 0; bi < 5; ++bi) {
         const Block bk = blocks[bi];
         float* dst = out + (size_t)bk.base * n + (size_t)bk.width * g0;
         const uint32_t total = bk.width * cnt;
         for (uint32_t i = threadIdx.x; i < total; i += kBwdGroup) {
             const float v = zero ? 0.0f : tile[bk.row + i % bk.width][i / bk.width];
             dst[i] = add ? dst[i] + v : v;
+        }
+    }
+    constexpr uint32_t kRest = kRows - kRowRest;  // 45
+    static_assert(kRest > 32 && kRest <= 64, "two row passes cover f_rest");
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    float* dst = out + (size_t)14 * n + (size_t)kRest * g0;
+    for (uint32_t task = warp; task < 2u * (kBwdGroup / 4u); task += kBwdGroup / 32u) {
+        const uint32_t r = (task & 1u) * 32u + lane;  // f_rest row
+        const uint32_t c0 = (task >> 1) * 4u;          // first of four Gaussians (column)
+        if (r >= kRest || c0 >= cnt) continue;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!zero) v = *reinterpret_cast<const float4*>(&tile[kRowRest + r][c0]);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (uint32_t k = 0; k < 4u; ++k) {
+            if (c0 + k >= cnt) break;
+            float* p = dst + (size_t)(c0 + k) * kRest + r;
+            *p = add ? *p + vv[k] : vv[k];
         }
     }
 }
