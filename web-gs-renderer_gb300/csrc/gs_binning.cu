@@ -367,7 +367,6 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     __shared__ uint32_t s_vals[PART];
     __shared__ uint32_t s_whist[WARPS][RADIX];
     __shared__ uint32_t s_gbase[RADIX];     // global exclusive digit base of this pass
-    __shared__ uint32_t s_dstart[RADIX];    // local sorted start of each digit
     __shared__ uint32_t s_out[RADIX];       // global position of local element 0 of each digit
     __shared__ uint32_t s_warp[WARPS + 1];
     __shared__ uint32_t s_part, s_seq;
@@ -439,7 +438,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
         uint32_t dtot;
         const uint32_t dstart = block_exclusive_scan<kSortThreads>(tid < RADIX ? cta_total : 0u, s_warp, &dtot);
         if (tid < RADIX) {
-            s_dstart[tid] = dstart;
+            // each warp's slot base of this digit: the digit's local sorted start plus the warps before
+#pragma unroll
+            for (uint32_t w = 0; w < WARPS; ++w) s_whist[w][tid] += dstart;
             // lookback per digit (one thread per digit, bounded waits): the words of the next
             // kLookWidth predecessors are loaded together, so a walk over partitions that have only
             // published aggregates costs one memory round trip per kLookWidth steps
@@ -487,7 +488,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             const uint32_t idx = wbase + k * 32u + lane;
             if (idx < n) {
                 const uint32_t d = (key[k] >> shift) & MASK;
-                const uint32_t pos = s_dstart[d] + s_whist[warp][d] + rank[k];
+                const uint32_t pos = s_whist[warp][d] + rank[k];
                 s_keys[pos] = key[k];
                 s_vals[pos] = vals_in[idx];
             }
