@@ -8,6 +8,8 @@
 // Ordering: every kernel that chains partitions takes a ticket from FrameCtl so that partition p
 // only ever waits on partitions already owned by running CTAs; every wait is bounded
 // (warp_lookback).
+#include <algorithm>
+
 #include "gs_kernels.h"
 
 namespace gs {
@@ -71,7 +73,12 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
 __global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words) {
     pdl_wait();
     const uint32_t t = threadIdx.x;
-    for (uint32_t i = t; i < range_words; i += blockDim.x) ranges[i] = 0u;  // ranges cleared (renderer.js:919)
+    // tile ranges cleared (renderer.js:919): 16-byte stores across the grid, the tail word by word
+    const uint32_t quads = range_words / 4u;
+    for (uint32_t q = blockIdx.x * blockDim.x + t; q < quads; q += gridDim.x * blockDim.x)
+        reinterpret_cast<uint4*>(ranges)[q] = make_uint4(0u, 0u, 0u, 0u);
+    if (blockIdx.x != 0) return;
+    for (uint32_t i = quads * 4u + t; i < range_words; i += blockDim.x) ranges[i] = 0u;
     if (t == 0) {
         ctl->seq = (ctl->seq & ~15u) + 16u;
         ctl->status = 0u;
@@ -624,7 +631,10 @@ int sm_count() {
 }  // namespace
 
 void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges, uint32_t range_words) {
-    launch_pdl(k_frame_begin, dim3(1), dim3(1024), s, ctl, ranges, range_words);
+    // ranges come from cudaMalloc (16-byte aligned); one 16-byte store per thread, up to 64 CTAs
+    const uint32_t quads = range_words / 4u;
+    const uint32_t grid = std::max(1u, std::min(64u, (quads + 255u) / 256u));
+    launch_pdl(k_frame_begin, dim3(grid), dim3(256), s, ctl, ranges, range_words);
 }
 
 void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uint32_t tiles_x, uint32_t max_instance,
