@@ -202,6 +202,23 @@ def test_repeat_frames_are_deterministic(gpu_ctx):
     np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
 
 
+@pytest.mark.parametrize("flags", [webgs.GS_FLAG_NO_GRAPH, webgs.GS_FLAG_PROFILE])
+def test_eager_launches_match_oracle(flags):
+    """Frames launched eagerly (no graph; and the profiling context, with events between the passes)
+    chain their kernels as programmatic dependent launches, as the captured graph does: the result is
+    the oracle's, bit for bit, on repeated frames."""
+    packed = W.SceneSpec(60_000, 12, 0).build()
+    view = W.CameraSpec((0.3, 0.2, -3.8), (0.0, 0.0, 0.0), 60.0, 400, 300).view()
+    o = oracle_frame(view, packed, 60_000)
+    with webgs.Context(flags=flags) as ctx:
+        scene = ctx.upload(packed, 60_000)
+        try:
+            for _ in range(3):
+                assert_frame_parity(gpu_frame(ctx, scene, view), o)
+        finally:
+            scene.close()
+
+
 def test_scene_scale_config_parity(gpu_ctx):
     """1M Gaussians, 64-cluster mixture in a 20^3 box, 1920x1080, camera inside the box."""
     packed = W.SCENE_1M.build()

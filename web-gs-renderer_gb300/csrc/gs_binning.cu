@@ -9,6 +9,7 @@
 // only ever waits on partitions already owned by running CTAs; every wait is bounded
 // (warp_lookback).
 #include <algorithm>
+#include <atomic>
 
 #include "gs_kernels.h"
 
@@ -617,15 +618,19 @@ __global__ void __launch_bounds__(1024) k_tile_order(const uint32_t* __restrict_
     }
 }
 
+// SM count of the current device (contexts of one process share a GPU model; read once, and from
+// any thread).
 int sm_count() {
-    static int cached = 0;
-    if (cached == 0) {
-        int dev = 0, v = 0;
+    static std::atomic<int> cached{0};
+    int v = cached.load(std::memory_order_relaxed);
+    if (v == 0) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        cached = v > 0 ? v : 1;
+        v = v > 0 ? v : 1;
+        cached.store(v, std::memory_order_relaxed);
     }
-    return cached;
+    return v;
 }
 
 }  // namespace
