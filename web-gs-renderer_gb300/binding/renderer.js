@@ -1,6 +1,8 @@
 // renderer.js -- drop-in for src/renderer/renderer.js backed by libwebgs.so through the N-API addon.
 // Same public methods (constructor, uploadGsData, setGs, execute); the WebGPU device, canvas and blit
-// are replaced by a headless rgba8 image (this.image) of {width, height}.
+// are replaced by a headless rgba8 image (this.image) the size of a canvas-like {width, height} object,
+// which is read every frame as the reference reads its canvas (renderer.js #resize): changing its
+// width or height resizes the camera and the image and forces the next frame.
 import {createRequire} from "module";
 import {Camera} from "../src/renderer/camera.js";  // the reference camera, unchanged (binding folder placed at native/ in that tree)
 
@@ -8,17 +10,18 @@ const require = createRequire(import.meta.url);
 const {Native} = require("./build/Release/webgs.node");
 
 export class Renderer {
-    #native; #camera; #onProfile; #width; #height; #lastTime; #previousGs; #currentGs; #isResized = true;
+    #native; #camera; #onProfile; #canvas; #width; #height; #lastTime; #previousGs; #currentGs; #isResized = true;
     #names = new Set();
 
-    // device/context/format of the WebGPU constructor become {width, height}
-    constructor({width, height}, _context, _format, onProfile) {
+    // device/context/format of the WebGPU constructor become a canvas-like {width, height}
+    constructor(canvas, _context, _format, onProfile) {
         this.#native = new Native({profile: !!onProfile});
         this.#onProfile = onProfile;
-        this.#width = width;
-        this.#height = height;
-        this.#camera = new Camera(width, height);
-        this.image = new Uint8Array(width * height * 4);
+        this.#canvas = canvas;
+        this.#width = canvas.width;
+        this.#height = canvas.height;
+        this.#camera = new Camera(this.#width, this.#height);
+        this.image = new Uint8Array(this.#width * this.#height * 4);
     }
 
     uploadGsData(data, name) {
@@ -35,6 +38,7 @@ export class Renderer {
         const now = performance.now();
         const dt = this.#lastTime === undefined ? 0 : (now - this.#lastTime) / 1000;
         this.#lastTime = now;
+        this.#resize();
         this.#camera.update(dt);
         if (!this.#names.has(this.#currentGs)) return;
         if (!this.#camera.pollDirty() && !this.#isResized && this.#currentGs === this.#previousGs) return;
@@ -47,5 +51,16 @@ export class Renderer {
         f.set(focal, 36); f.set(tanFov, 38); f.set([this.#width, this.#height], 40);
         this.#native.render(block, this.image);
         this.#onProfile?.(this.#native.timings());
+    }
+
+    // renderer.js #resize: a new canvas size resizes the camera and the output image
+    #resize() {
+        const {width, height} = this.#canvas;
+        if (width === this.#width && height === this.#height) return;
+        this.#width = width;
+        this.#height = height;
+        this.#camera.resize(width, height);
+        this.image = new Uint8Array(width * height * 4);
+        this.#isResized = true;
     }
 }
