@@ -521,6 +521,22 @@ def batched_forward(steps, warmup, local_rank) -> dict:
             res[label]["per_view_plain"] = per_view
             res[label]["largest_scene_views_ms"] = round(big, 4)
             res[label]["overlap_bound_batched_over_plain"] = round(sum(v["ms"] for v in per_view) / big, 3)
+            # per-pass times of the same 16 frames (profiling context, events between the passes): the
+            # raster, issue-bound at full residency on the large views, is the part a batch cannot share
+            pctx = webgs.Context(device=local_rank, flags=webgs.GS_FLAG_PROFILE)
+            pscs = [pctx.upload(p, s.count) for s, p in zip(W.BATCH_SCENES, packs)]
+            acc = {}
+            for rep in range(3):
+                for k, (si, _) in enumerate(cams):
+                    pctx.forward_device(pscs[si], views[k], rgba8=imgs[k].data_ptr())
+                    if rep == 2:
+                        for name, v in pctx.timings().items():
+                            acc[name] = acc.get(name, 0.0) + v["ms"]
+            for sc_ in pscs:
+                sc_.close()
+            pctx.close()
+            res[label]["passes_ms_sum_16_views"] = {k: round(v, 4) for k, v in acc.items()}
+            res[label]["raster_share_plain"] = round(acc.get("raster", 0.0) / max(acc.get("TOTAL", 1e-9), 1e-9), 3)
             # end to end: every view's rgba8 image lands in pinned host memory; plain = one synchronous
             # gs_forward per view (one Renderer.execute() per view), batched = one gs_forward_batch
             hosts = [torch.empty(c.width * c.height * 4, dtype=torch.uint8, pin_memory=True) for _, c in cams]
