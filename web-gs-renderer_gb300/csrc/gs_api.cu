@@ -120,6 +120,7 @@ struct gs_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t side[kSideStreams] = {};
     cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+    cudaEvent_t group_done[kSideStreams] = {};  // a batch's per-scene preprocess, one per group
     std::string err;
 
     Frame main;                  // gs_forward / gs_backward
@@ -357,39 +358,50 @@ int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, con
         if (frames.size() == 1) {
             enqueue_frame(ctx, *frames[0], args[0], ctx->stream, false);
         } else {
-            // views of one scene are preprocessed together (one pass over the scene's attributes per
-            // group of up to 16 views), on the main stream before the fork
-            std::vector<char> pre(frames.size(), 0);
-            for (size_t i = 0; i < frames.size(); ++i) {
-                if (pre[i]) continue;
-                std::vector<size_t> group;
+            // views are independent: fork them over the side streams so small views fill the GPU
+            // together. Views of one scene are preprocessed together (one pass over the scene's
+            // attributes per group of up to 16 views) on the stream of the group's first view, so the
+            // groups' preprocesses run side by side; a view on another stream waits for its group.
+            cudaEventRecord(ctx->fork, ctx->stream);
+            const int used = (int)std::min<size_t>(frames.size(), kSideStreams);
+            for (int s = 0; s < used; ++s) cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0);
+            std::vector<int> group_of(frames.size(), -1);
+            int groups = 0;
+            for (size_t i = 0; i < frames.size() && groups < kSideStreams; ++i) {
+                if (group_of[i] >= 0) continue;
+                std::vector<size_t> members;
                 for (size_t j = i; j < frames.size(); ++j)
-                    if (!pre[j] && args[j].scene == args[i].scene) group.push_back(j);
-                if (group.size() < 2) continue;
-                for (size_t c0 = 0; c0 < group.size(); c0 += kMaxMultiViews) {
+                    if (group_of[j] < 0 && args[j].scene == args[i].scene) members.push_back(j);
+                if (members.size() < 2) continue;
+                for (size_t c0 = 0; c0 < members.size() && groups < kSideStreams; c0 += kMaxMultiViews) {
                     MultiViewFrames mv{};
-                    mv.count = (uint32_t)std::min<size_t>(kMaxMultiViews, group.size() - c0);
+                    mv.count = (uint32_t)std::min<size_t>(kMaxMultiViews, members.size() - c0);
                     for (uint32_t v = 0; v < mv.count; ++v) {
-                        const size_t j = group[c0 + v];
+                        const size_t j = members[c0 + v];
                         Frame& f = *frames[j];
-                        launch_frame_begin(f.ctl.p, ctx->stream, f.ranges.p, args[j].tiles_x * args[j].tiles_y * 2u);
                         mv.view[v] = args[j].view;
                         mv.rec[v] = f.rec.p;
                         mv.meta[v] = f.meta.p;
                         mv.counts[v] = f.counts.p;
                         mv.ctl[v] = f.ctl.p;
-                        pre[j] = 1;
+                        mv.ranges[v] = f.ranges.p;
+                        mv.range_words[v] = args[j].tiles_x * args[j].tiles_y * 2u;
+                        group_of[j] = groups;
                     }
+                    cudaStream_t gs = ctx->side[members[c0] % used];
+                    launch_frame_begin_multi(mv, gs);
                     launch_preprocess_multi(args[i].scene->rows, args[i].scene->stride, args[i].n,
-                                            ctx->cfg.tile_size, mv, ctx->stream);
+                                            ctx->cfg.tile_size, mv, gs);
+                    cudaEventRecord(ctx->group_done[groups], gs);
+                    ++groups;
                 }
             }
-            // views are independent: fork them over the side streams so small views fill the GPU together
-            cudaEventRecord(ctx->fork, ctx->stream);
-            const int used = (int)std::min<size_t>(frames.size(), kSideStreams);
-            for (int s = 0; s < used; ++s) cudaStreamWaitEvent(ctx->side[s], ctx->fork, 0);
-            for (size_t i = 0; i < frames.size(); ++i)
-                enqueue_frame(ctx, *frames[i], args[i], ctx->side[i % used], false, pre[i] != 0);
+            for (size_t i = 0; i < frames.size(); ++i) {
+                cudaStream_t s = ctx->side[i % used];
+                const int g = group_of[i];
+                if (g >= 0) cudaStreamWaitEvent(s, ctx->group_done[g], 0);
+                enqueue_frame(ctx, *frames[i], args[i], s, false, g >= 0);
+            }
             for (int s = 0; s < used; ++s) {
                 cudaEventRecord(ctx->join[s], ctx->side[s]);
                 cudaStreamWaitEvent(ctx->stream, ctx->join[s], 0);
@@ -461,7 +473,8 @@ int gs_ctx_create(const gs_config* cfg, gs_ctx** out) {
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int s = 0; ok && s < kSideStreams; ++s)
         ok = cudaStreamCreateWithFlags(&ctx->side[s], cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreateWithFlags(&ctx->join[s], cudaEventDisableTiming) == cudaSuccess;
+             cudaEventCreateWithFlags(&ctx->join[s], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->group_done[s], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) == cudaSuccess &&
          cudaEventCreateWithFlags(&ctx->bviews_done, cudaEventDisableTiming) == cudaSuccess &&
          ctx->main.init(ctx->stream) == cudaSuccess && ctx->aux_ctl.reserve(1) == cudaSuccess &&
@@ -498,6 +511,7 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     for (int s = 0; s < kSideStreams; ++s) {
         if (ctx->side[s]) cudaStreamDestroy(ctx->side[s]);
         if (ctx->join[s]) cudaEventDestroy(ctx->join[s]);
+        if (ctx->group_done[s]) cudaEventDestroy(ctx->group_done[s]);
     }
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->bviews_done) cudaEventDestroy(ctx->bviews_done);

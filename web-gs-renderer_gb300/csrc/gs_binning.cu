@@ -71,14 +71,15 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
     return r;
 }
 
-__global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words) {
-    pdl_wait();
+// Resets one frame's control block (CTA 0) and clears its tile ranges (renderer.js:919) with
+// 16-byte stores across the CTAs [0, ncta), the tail word by word.
+__device__ __forceinline__ void frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words, uint32_t cta,
+                                            uint32_t ncta) {
     const uint32_t t = threadIdx.x;
-    // tile ranges cleared (renderer.js:919): 16-byte stores across the grid, the tail word by word
     const uint32_t quads = range_words / 4u;
-    for (uint32_t q = blockIdx.x * blockDim.x + t; q < quads; q += gridDim.x * blockDim.x)
+    for (uint32_t q = cta * blockDim.x + t; q < quads; q += ncta * blockDim.x)
         reinterpret_cast<uint4*>(ranges)[q] = make_uint4(0u, 0u, 0u, 0u);
-    if (blockIdx.x != 0) return;
+    if (cta != 0) return;
     for (uint32_t i = quads * 4u + t; i < range_words; i += blockDim.x) ranges[i] = 0u;
     if (t == 0) {
         ctl->seq = (ctl->seq & ~15u) + 16u;
@@ -90,6 +91,17 @@ __global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_wo
     }
     if (t < 15) ctl->tickets[t] = 0u;
     for (uint32_t i = t; i < 8u * 256u; i += blockDim.x) ctl->hist[i] = 0u;
+}
+
+__global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words) {
+    pdl_wait();
+    frame_begin(ctl, ranges, range_words, blockIdx.x, gridDim.x);
+}
+
+__global__ void k_frame_begin_multi(MultiViewFrames mv) {
+    pdl_wait();
+    const uint32_t v = blockIdx.y;
+    frame_begin(mv.ctl[v], mv.ranges[v], mv.range_words[v], blockIdx.x, gridDim.x);
 }
 
 // ---- fused offset scan + emit ---------------------------------------------------------------
@@ -634,6 +646,13 @@ int sm_count() {
 }
 
 }  // namespace
+
+void launch_frame_begin_multi(const MultiViewFrames& mv, cudaStream_t s) {
+    uint32_t quads = 0;
+    for (uint32_t v = 0; v < mv.count; ++v) quads = std::max(quads, mv.range_words[v] / 4u);
+    const uint32_t grid = std::max(1u, std::min(64u, (quads + 255u) / 256u));
+    launch_pdl(k_frame_begin_multi, dim3(grid, mv.count), dim3(256), s, mv);
+}
 
 void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges, uint32_t range_words) {
     // ranges come from cudaMalloc (16-byte aligned); one 16-byte store per thread, up to 64 CTAs

@@ -51,8 +51,12 @@ struct MultiViewFrames {
     uint4* meta[kMaxMultiViews];
     uint32_t* counts[kMaxMultiViews];
     FrameCtl* ctl[kMaxMultiViews];
+    uint32_t* ranges[kMaxMultiViews];  // tile ranges, cleared by launch_frame_begin_multi
+    uint32_t range_words[kMaxMultiViews];
     uint32_t count;
 };
+// launch_frame_begin for every view of mv in one launch (one row of CTAs per view).
+void launch_frame_begin_multi(const MultiViewFrames& mv, cudaStream_t s);
 // The preprocess of several views of one scene in one pass over the scene's attribute rows (each
 // view's FrameCtl must have been reset by launch_frame_begin).
 void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uint32_t tile, const MultiViewFrames& mv,
