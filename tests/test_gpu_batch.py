@@ -41,6 +41,23 @@ def test_batch_equals_single_views(scenes):
     np.testing.assert_array_equal(batch[0]["rgb"].view(np.uint32), o["rgb"].view(np.uint32))
 
 
+def test_batch_of_twenty_views_of_one_scene(scenes):
+    """More views than side streams and than one shared preprocess takes (16): the scene's views
+    are preprocessed in two groups and four streams carry two views each; every view equals its
+    single frame bit for bit."""
+    specs, packs = scenes
+    cams = W.orbit_cameras(20, 17, 9.0, resolutions=((96, 64), (128, 96)))
+    with webgs.Context() as ctx:
+        sc = ctx.upload(packs[1], specs[1].count)
+        items = [(sc, cam.view()) for _, cam in cams]
+        batch = ctx.forward_batch(items, rgba8=True, rgb=True)
+        for (scene, view), b in zip(items, batch):
+            single = ctx.forward(scene, view, rgba8=True, rgb=True)
+            np.testing.assert_array_equal(b["rgb"].view(np.uint32), single["rgb"].view(np.uint32))
+            np.testing.assert_array_equal(b["rgba8"], single["rgba8"])
+        sc.close()
+
+
 @pytest.mark.parametrize("views,w,h", [(3, 256, 192), (18, 96, 64)])
 def test_batch_backward_is_sum_of_views(views, w, h):
     """The batched backward (one preprocess backward per group of up to 16 views, the later groups
