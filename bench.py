@@ -128,11 +128,11 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu --set full capture of
 # the forward frame of this workload on a GB300) and what bounds each kernel there.
-NCU_TRAFFIC_BYTES = {"preprocess": 287.2e6, "raster": 56.5e6}
+NCU_TRAFFIC_BYTES = {"preprocess": 286.4e6, "raster": 56.4e6}
 LIMITER = {
-    "raster": "instruction issue (ncu: issue slots busy 93.5% at full residency, DRAM 2% of peak; the "
+    "raster": "instruction issue (ncu: issue slots busy 93.9% at full residency, DRAM 2% of peak; the "
               "48-byte records are re-read from L2, so DRAM traffic is below the algorithmic bytes)",
-    "preprocess": "HBM (ncu: 69% of DRAM peak, stalls on the bulk-copy wait)",
+    "preprocess": "HBM and the pinned arithmetic (ncu: 70% of DRAM peak, 68% of issue slots)",
 }
 
 
