@@ -1,13 +1,16 @@
 // gs_binning.cu -- offset scan, emit, radix sort and tile ranges of the splat pipeline:
-//   offset scan  src/shaders/offset_scan.wgsl:22-67   -> k_scan_emit (single-pass decoupled lookback)
+//   offset scan  src/shaders/offset_scan.wgsl:22-67   -> k_scan_emit (single pass: each partition sums
+//                                                        its predecessors' published aggregates)
 //   emit         src/shaders/emit.wgsl:28-66          -> k_scan_emit (fused, load-balanced)
 //   indirect arg src/shaders/indirect_arg.wgsl:14-27  -> FrameCtl counts read on the device
-//   radix sort   src/shaders/radix_parallel.wgsl      -> k_onesweep (one kernel per digit pass)
+//   radix sort   src/shaders/radix_parallel.wgsl      -> k_onesweep (one kernel per digit pass,
+//                                                        decoupled lookback per digit)
 //   tile ranges  src/shaders/tile_ranges.wgsl:7-34    -> k_tile_ranges
+//   range clear  renderer.js:919                      -> k_frame_begin(_multi) (with the counters reset)
 //
 // Ordering: every kernel that chains partitions takes a ticket from FrameCtl so that partition p
-// only ever waits on partitions already owned by running CTAs; every wait is bounded
-// (warp_lookback).
+// only ever waits on partitions already owned by running CTAs; every wait is bounded (kSpinLimit
+// polls, then the timeout status is set and the wait ends).
 #include <algorithm>
 #include <atomic>
 
