@@ -57,8 +57,10 @@ __device__ __forceinline__ float4 cull_box(float x, float y, float a, float b, f
     const float det_lo = (ac - bb) - 4.0f * 0x1p-24f * (ac + bb);
     if (!(det_lo > 0.0f)) return keep_all;
     const float k = (-2.0f * cut + 0x1p-20f * smax) * 1.000001f;
-    const float hx = sqrtf(k * c / det_lo) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
-    const float hy = sqrtf(k * a / det_lo) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
+    // approximate divide and square root (a few ulp), far inside the 1e-5 relative margin
+    const float vx = __fdividef(k * c, det_lo), vy = __fdividef(k * a, det_lo);
+    const float hx = vx * rsqrtf(vx) * 1.00001f + 1.0e-3f + fabsf(x) * 0x1p-22f;
+    const float hy = vy * rsqrtf(vy) * 1.00001f + 1.0e-3f + fabsf(y) * 0x1p-22f;
     if (!finite_f(hx) || !finite_f(hy)) return keep_all;
     return make_float4(x - hx, x + hx, y - hy, y + hy);
 }
