@@ -129,6 +129,9 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu --set full capture of
 # the forward frame of this workload on a GB300) and what bounds each kernel there.
 NCU_TRAFFIC_BYTES = {"preprocess": 286.4e6, "raster": 56.4e6}
+# issue-slot utilisation of the kernels bound by instruction issue (ncu smsp__issue_active, the same
+# capture): for them this, not the HBM fraction, is the efficiency measure
+NCU_ISSUE_ACTIVE = {"raster": 0.939}
 LIMITER = {
     "raster": "instruction issue (ncu: issue slots busy 93.9% at full residency, DRAM 2% of peak; the "
               "48-byte records are re-read from L2, so DRAM traffic is below the algorithmic bytes)",
@@ -330,7 +333,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     achieved = bytes_per[top] / (kernel_passes[top] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get(top), "peak_source": peak_kind,
-            "algorithmic_bytes": int(bytes_per[top]), "limiter": LIMITER.get(top)}
+            "algorithmic_bytes": int(bytes_per[top]), "limiter": LIMITER.get(top),
+            "issue_active_ncu": NCU_ISSUE_ACTIVE.get(top)}
     per_pass = {k: {"ms": round(v, 4), "bytes": int(bytes_per.get(k, 0)),
                     "GBps": round(bytes_per.get(k, 0) / (v * 1e-3) / 1e9, 1) if v > 0 and k in bytes_per else None}
                 for k, v in pass_ms.items()}
