@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
     __shared__ float4 s_b[BATCH];
     __shared__ float2 s_c[BATCH];
     __shared__ float4 s_box[BATCH];
+    __shared__ float4 s_diag[BATCH];
     __shared__ uint32_t s_g[BATCH];
     __shared__ uint32_t s_maxl;
 
@@ -193,11 +194,12 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                 s_a[j] = r0;
                 s_b[j] = r1;
                 s_c[j] = make_float2(r2.x, r2.y);
-                s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1, s_diag[j]);
                 s_g[j] = g;
             } else {
                 const float inf = __int_as_float(0x7f800000);
                 s_box[j] = make_float4(inf, -inf, inf, -inf);
+                s_diag[j] = s_box[j];
                 s_g[j] = 0xFFFFFFFFu;
             }
         }
@@ -209,7 +211,8 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
             for (int gtop = top; gtop >= 0; gtop -= 32) {
                 const int gbase = gtop - 31;
                 const int jj = gbase + (int)lane;
-                const bool hit = jj >= 0 && box_meets(s_box[jj], rx0, rx1, ry0, ry1);
+                const bool hit = jj >= 0 && box_meets(s_box[jj], rx0, rx1, ry0, ry1) &&
+                                 box_meets(s_diag[jj], rx0 + ry0, rx1 + ry1, rx0 - ry1, rx1 - ry0);
                 uint32_t m = __ballot_sync(0xffffffffu, hit);
                 while (m) {
                     const int bit = 31 - __clz(m);

@@ -14,12 +14,13 @@
 //  * cut-off: a pixel whose power is below the splat's cut-off c_o = ln((1/255)/o) - 1e-3 skips
 //    the exp, since o*exp(power) < 1/255 is certain there (the 1e-3 margin is far beyond the
 //    rounding of exp, the product and logf);
-//  * warp cull: when staging a splat, the CTA computes the bounding box of the region of the tile
-//    where power >= c_o can hold (gs_raster_common.cuh gives the bound). Every warp tests its 8x4
-//    pixel block against the 32 boxes of a group in parallel (one box per lane, one ballot) and
-//    walks only the splats whose box meets its block, in range order. A skipped splat would have
-//    been rejected by every pixel of the warp at "power < c_o" (or "power > 0"). Contributor counts
-//    are range positions, so skipping does not change them.
+//  * warp cull: when staging a splat, the CTA computes an octagon (the bounding box and the
+//    45-degree box) around the region of the tile where power >= c_o can hold
+//    (gs_raster_common.cuh gives the bound). Every warp tests its 8x4 pixel block against the 32
+//    octagons of a group in parallel (one per lane, one ballot) and walks only the splats whose
+//    octagon meets its block, in range order. A skipped splat would have been rejected by every
+//    pixel of the warp at "power < c_o" (or "power > 0"). Contributor counts are range positions, so
+//    skipping does not change them.
 //
 // Full residency (2048 threads per SM, 32 registers; the few spilled bytes cost less than the lost
 // warps did).
@@ -47,6 +48,7 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
     __shared__ float4 s_b[BATCH];    // (conic.z, opacity, r, g)
     __shared__ float2 s_c[BATCH];    // (b, cut)
     __shared__ float4 s_box[BATCH];  // cull box (x0, x1, y0, y1)
+    __shared__ float4 s_diag[BATCH];  // its 45-degree box (u0, u1, v0, v1), u = x + y, v = x - y
 
     const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
@@ -79,13 +81,14 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
                     s_a[j] = r0;
                     s_b[j] = r1;
                     s_c[j] = make_float2(r2.x, r2.y);
-                    s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1);
+                    s_box[j] = cull_box(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, tx0, tx1, ty0, ty1, s_diag[j]);
                 } else {  // only after a timed-out sort: a splat that never blends
                     const float inf = __int_as_float(0x7f800000);
                     s_a[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     s_b[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     s_c[j] = make_float2(0.0f, inf);
                     s_box[j] = make_float4(inf, -inf, inf, -inf);
+                    s_diag[j] = s_box[j];
                 }
             }
         }
@@ -95,7 +98,9 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
         for (uint32_t g0 = 0; g0 < cnt; g0 += 32u) {
             if (__all_sync(0xffffffffu, done)) break;
             bool hit = false;
-            if (g0 + lane < cnt) hit = box_meets(s_box[g0 + lane], rx0, rx1, ry0, ry1);
+            if (g0 + lane < cnt)
+                hit = box_meets(s_box[g0 + lane], rx0, rx1, ry0, ry1) &&
+                      box_meets(s_diag[g0 + lane], rx0 + ry0, rx1 + ry1, rx0 - ry1, rx1 - ry0);
             uint32_t m = __ballot_sync(0xffffffffu, hit);
             while (m) {
                 const uint32_t j = g0 + (uint32_t)(__ffs(m) - 1);
