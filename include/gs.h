@@ -178,9 +178,9 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
 
 /* Autotuner (no counterpart in the reference, whose constants are fixed): times gs_forward_batch of
  * `views` over one scene for every tile size {8,16,32} x radix digit width {4,8} x raster batch
- * depth {32,64,128,256} x sort block {2048,4096}, `iters` frames each, and returns the fastest
- * configuration (other fields from `base`) and its ms per batch. Creates and destroys its own
- * contexts. */
+ * depth {32,64,128,256} x sort block {2048,4096}, `iters` batches each, re-times the three fastest
+ * with 4 x `iters` batches, and returns the fastest of those (other fields from `base`) with its ms
+ * per batch. Creates and destroys its own contexts. */
 int gs_autotune(const gs_config* base, const float* packed, uint32_t count, const gs_view* views, uint32_t n_views,
                 uint32_t iters, gs_config* best, float* best_ms);
 

@@ -1024,66 +1024,83 @@ int gs_autotune_scenes(const gs_config* base, const float* const* packed, const 
     gs_config b;
     gs_config_default(&b);
     if (base) b = *base;
+    // times one configuration on the whole batch (its own context and scene copies): ms per batch
+    auto time_config = [&](const gs_config& c, uint32_t reps, float* ms) -> int {
+        gs_ctx* ctx = nullptr;
+        if (gs_ctx_create(&c, &ctx) != GS_OK) return GS_ERR_CUDA;
+        std::vector<gs_scene*> scs(n_scenes, nullptr);
+        int rc = GS_OK;
+        for (uint32_t s = 0; rc == GS_OK && s < n_scenes; ++s)
+            rc = gs_scene_upload(ctx, packed[s], counts[s], GS_MEM_HOST, &scs[s]);
+        std::vector<gs_batch_view> bv(n_views);
+        std::vector<uint32_t*> imgs(n_views, nullptr);
+        for (uint32_t i = 0; rc == GS_OK && i < n_views; ++i) {
+            const size_t pix = (size_t)views[i].texture_size[0] * (size_t)views[i].texture_size[1];
+            if (cudaMalloc(&imgs[i], pix * 4) != cudaSuccess) rc = GS_ERR_OOM;
+            bv[i].scene = scs[view_scene ? view_scene[i] : 0];
+            bv[i].view = views[i];
+            bv[i].out = gs_image{GS_MEM_DEVICE, reinterpret_cast<uint8_t*>(imgs[i]), nullptr, nullptr, nullptr};
+        }
+        *ms = 0.0f;
+        if (rc == GS_OK) {
+            for (int w = 0; w < 2 && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++w)
+                rc = gs_forward_batch(ctx, bv.data(), n_views);
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, ctx->stream);
+            for (uint32_t k = 0; k < reps && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++k)
+                rc = gs_forward_batch(ctx, bv.data(), n_views);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(ms, e0, e1);
+            *ms /= (float)reps;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (rc == GS_OK || rc == GS_ERR_OVERFLOW) rc = gs_ctx_synchronize(ctx);
+        }
+        for (uint32_t* p : imgs)
+            if (p) cudaFree(p);
+        for (gs_scene* sc : scs)
+            if (sc) gs_scene_destroy(sc);
+        gs_ctx_destroy(ctx);
+        return rc == GS_ERR_OVERFLOW ? GS_OK : rc;
+    };
+    // every candidate with `iters` timed batches, then the three fastest again with four times as
+    // many: a close second of the first sweep is often the faster one
     const uint32_t tiles[] = {8, 16, 32};
     const uint32_t digits[] = {4, 8};
     const uint32_t batches[] = {32, 64, 128, 256};
     const uint32_t blocks[] = {kSortPartitionMin, kSortPartition};
-    float best_t = 3.0e38f;
-    gs_config best_c = b;
+    const uint32_t reps = std::max(iters, 1u);
+    std::vector<std::pair<float, gs_config>> timed;
     for (uint32_t t : tiles)
         for (uint32_t d : digits)
             for (uint32_t r : batches)
-            for (uint32_t sb : blocks) {
-                gs_config c = b;
-                c.tile_size = t;
-                c.digit_bits = d;
-                c.raster_batch = r;
-                c.sort_block = sb;
-                c.flags &= ~(GS_FLAG_PROFILE | GS_FLAG_DIFFERENTIABLE);
-                gs_ctx* ctx = nullptr;
-                if (gs_ctx_create(&c, &ctx) != GS_OK) return GS_ERR_CUDA;
-                std::vector<gs_scene*> scs(n_scenes, nullptr);
-                int rc = GS_OK;
-                for (uint32_t s = 0; rc == GS_OK && s < n_scenes; ++s)
-                    rc = gs_scene_upload(ctx, packed[s], counts[s], GS_MEM_HOST, &scs[s]);
-                std::vector<gs_batch_view> bv(n_views);
-                std::vector<uint32_t*> imgs(n_views, nullptr);
-                for (uint32_t i = 0; rc == GS_OK && i < n_views; ++i) {
-                    const size_t pix = (size_t)views[i].texture_size[0] * (size_t)views[i].texture_size[1];
-                    if (cudaMalloc(&imgs[i], pix * 4) != cudaSuccess) rc = GS_ERR_OOM;
-                    bv[i].scene = scs[view_scene ? view_scene[i] : 0];
-                    bv[i].view = views[i];
-                    bv[i].out = gs_image{GS_MEM_DEVICE, reinterpret_cast<uint8_t*>(imgs[i]), nullptr, nullptr, nullptr};
+                for (uint32_t sb : blocks) {
+                    gs_config c = b;
+                    c.tile_size = t;
+                    c.digit_bits = d;
+                    c.raster_batch = r;
+                    c.sort_block = sb;
+                    c.flags &= ~(GS_FLAG_PROFILE | GS_FLAG_DIFFERENTIABLE);
+                    float ms = 0.0f;
+                    const int rc = time_config(c, reps, &ms);
+                    if (rc != GS_OK) return rc;
+                    timed.emplace_back(ms, c);
                 }
-                float ms = 0.0f;
-                if (rc == GS_OK) {
-                    for (int w = 0; w < 2 && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++w)
-                        rc = gs_forward_batch(ctx, bv.data(), n_views);
-                    cudaEvent_t e0, e1;
-                    cudaEventCreate(&e0);
-                    cudaEventCreate(&e1);
-                    cudaEventRecord(e0, ctx->stream);
-                    for (uint32_t k = 0; k < std::max(iters, 1u) && (rc == GS_OK || rc == GS_ERR_OVERFLOW); ++k)
-                        rc = gs_forward_batch(ctx, bv.data(), n_views);
-                    cudaEventRecord(e1, ctx->stream);
-                    cudaEventSynchronize(e1);
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    ms /= (float)std::max(iters, 1u);
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    if (rc == GS_OK || rc == GS_ERR_OVERFLOW) rc = gs_ctx_synchronize(ctx);
-                }
-                for (uint32_t* p : imgs)
-                    if (p) cudaFree(p);
-                for (gs_scene* sc : scs)
-                    if (sc) gs_scene_destroy(sc);
-                gs_ctx_destroy(ctx);
-                if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return rc;
-                if (ms < best_t) {
-                    best_t = ms;
-                    best_c = c;
-                }
-            }
+    std::sort(timed.begin(), timed.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+    float best_t = 3.0e38f;
+    gs_config best_c = b;
+    for (size_t k = 0; k < std::min<size_t>(3, timed.size()); ++k) {
+        float ms = 0.0f;
+        const int rc = time_config(timed[k].second, 4 * reps, &ms);
+        if (rc != GS_OK) return rc;
+        if (ms < best_t) {
+            best_t = ms;
+            best_c = timed[k].second;
+        }
+    }
     best_c.flags = b.flags;
     *best = best_c;
     if (best_ms) *best_ms = best_t;
