@@ -2,7 +2,7 @@
 // reference, which only renders):
 //   k_raster_backward     per tile, walks each pixel's blended splats back to front from its last
 //                         contributor, recomputing power and alpha bit for bit as the forward did
-//                         (same pinned arithmetic, the forward's warp cull box), recovering T by
+//                         (same pinned arithmetic, the forward's warp cull octagon), recovering T by
 //                         division, and accumulating dL/d(pixel.xy, conic, opacity, colour) per
 //                         Gaussian: two pixels per lane, the warp reduces by shuffles, nine lanes
 //                         issue the atomics.
