@@ -98,3 +98,38 @@ def test_backward_needs_a_differentiable_forward(gpu_ctx):
         with pytest.raises(webgs.GsError):
             ctx.backward(b, np.zeros((64, 64, 3), np.float32))
         a.close(); b.close()
+
+
+def test_backward_hostile_inputs():
+    """The hostile scene of the forward test (zero quaternions, extreme scales and opacities,
+    Gaussians at the eye and on the near plane, huge colours) through forward, backward and the
+    FP64 adjoint: no fault, and the gradients of the ordinary Gaussians are finite and agree with
+    the adjoint (the hostile ones may carry NaN in both)."""
+    from test_gpu_hostile import _hostile_scene
+
+    n, seed = 10_000, 43
+    packed = _hostile_scene(n, seed)
+    hostile = np.random.default_rng(seed).permutation(n)[:1400]
+    ordinary = np.ones(n, bool)
+    ordinary[hostile] = False
+    view = W.CameraSpec((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 60.0, 320, 240).view()
+    dl = np.random.default_rng(7).normal(0.0, 1e-3, (240, 320, 3)).astype(np.float32)
+    with webgs.Context(flags=webgs.GS_FLAG_DIFFERENTIABLE) as ctx:
+        sc = ctx.upload(packed, n)
+        try:
+            ctx.forward(sc, view, rgba8=False, rgb=True, allow_overflow=True)
+            g32 = ctx.backward(sc, dl)
+        finally:
+            sc.close()
+    g64, _ = oracle.backward_f64(webgs.view_bytes(view), packed, n, dl)
+    for name, (a, b) in _groups(n).items():
+        width = (b - a) // n
+        x = g32[a:b].reshape(n, width)[ordinary].astype(np.float64).ravel()
+        y = g64[a:b].reshape(n, width)[ordinary].ravel()
+        assert np.isfinite(x).all(), name
+        ny = np.linalg.norm(y)
+        if ny == 0.0:
+            assert np.abs(x).max() == 0.0, name
+            continue
+        cos = float(x @ y / (np.linalg.norm(x) * ny))
+        assert cos >= 0.999, (name, cos, np.linalg.norm(x - y) / ny)
