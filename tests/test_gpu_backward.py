@@ -133,3 +133,23 @@ def test_backward_hostile_inputs():
             continue
         cos = float(x @ y / (np.linalg.norm(x) * ny))
         assert cos >= 0.999, (name, cos, np.linalg.norm(x - y) / ny)
+
+
+def test_repeated_backward_calls_do_not_accumulate():
+    """The 2D gradient buffer is cleared by the preprocess backward that consumed it, not by a memset
+    before each call: gradients of repeated calls, and of a scene after another of a different size,
+    equal the first call's (up to the order of the atomic sums)."""
+    a_spec, b_spec = W.SceneSpec(3000, 31, 0), W.SceneSpec(1200, 32, 0)
+    view = W.CameraSpec((0.1, 0.2, -4.0), (0, 0, 0), 60.0, 160, 120).view()
+    dl = np.random.default_rng(3).normal(0.0, 1e-3, (120, 160, 3)).astype(np.float32)
+    with webgs.Context(flags=webgs.GS_FLAG_DIFFERENTIABLE) as ctx:
+        a = ctx.upload(a_spec.build(), a_spec.count)
+        b = ctx.upload(b_spec.build(), b_spec.count)
+        runs = []
+        for sc in (a, a, b, a, b):
+            ctx.forward(sc, view, rgba8=False, rgb=True)
+            runs.append(ctx.backward(sc, dl))
+        a.close(); b.close()
+    for ref, other in ((runs[0], runs[1]), (runs[0], runs[3]), (runs[2], runs[4])):
+        scale = np.abs(ref).max()
+        assert scale > 0 and np.abs(other - ref).max() <= 1e-5 * scale

@@ -66,6 +66,7 @@ struct Frame {
     DevBuf<uint32_t> rgba8, n_contrib;
     DevBuf<float> rgb, final_t;
     DevBuf<float> grad2d, dl_stage;
+    bool grad2d_zero = false;  // grad2d holds zeros (cleared by the last preprocess backward)
     // the last frame rendered into these buffers
     const gs_scene* scene = nullptr;
     const ViewBlock* view_used = nullptr;  // device view block the last frame read
@@ -849,8 +850,12 @@ int gs_get_timings(gs_ctx* ctx, gs_timing* rows, int32_t max_rows, int32_t* n_ro
 // Raster backward of frame f into f.grad2d (dL/d of its per-Gaussian 2D quantities).
 static int enqueue_raster_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const float* dl, cudaStream_t s,
                                    cudaEvent_t* ev = nullptr) {
+    const float* before = f.grad2d.p;
     GS_CK(f.grad2d.reserve((size_t)scene->n * 9 + 4));  // + 4: the preprocess backward copies whole 16-byte units
-    if (scene->n) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, (size_t)scene->n * 9 * sizeof(float), s));
+    if (f.grad2d.p != before) f.grad2d_zero = false;
+    // the preprocess backward clears what it read, so a buffer that went through one needs no memset
+    if (scene->n && !f.grad2d_zero) GS_CK(cudaMemsetAsync(f.grad2d.p, 0, f.grad2d.cap * sizeof(float), s));
+    f.grad2d_zero = false;
     if (ev) cudaEventRecord(ev[0], s);
     launch_raster_backward(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[f.sorted_buf].p, f.rec.p,
                            scene->n, f.ctl.p, f.width, f.height, f.tiles_x, f.tiles_y, f.final_t.p, f.n_contrib.p, dl,
@@ -870,6 +875,7 @@ static int enqueue_backward(gs_ctx* ctx, Frame& f, const gs_scene* scene, const 
                                &f.ctl.p->status, s);
     if (ev) cudaEventRecord(ev[2], s);
     GS_CK(cudaGetLastError());
+    f.grad2d_zero = true;
     return GS_OK;
 }
 
@@ -964,6 +970,7 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
                                          &ctx->batch[g0]->ctl.p->status, ctx->stream);
     }
     GS_CK(cudaGetLastError());
+    for (uint32_t i = 0; i < count; ++i) ctx->batch[i]->grad2d_zero = true;
     for (uint32_t i = 0; i < count; ++i) {
         Frame& f = *ctx->batch[i];
         GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));

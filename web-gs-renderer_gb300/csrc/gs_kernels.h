@@ -122,7 +122,7 @@ void launch_raster_backward(uint32_t tile, uint32_t batch, const uint32_t* range
 struct MultiViewGrads {
     const ViewBlock* view[kMaxMultiViews];
     const uint32_t* counts[kMaxMultiViews];
-    const float* grad2d[kMaxMultiViews];
+    float* grad2d[kMaxMultiViews];  // cleared after use (the raster backward accumulates into zeros)
     uint32_t count;
 };
 // Sum over the views of their dL/d(attributes), written in the packed layout into `out` (add: added
@@ -134,7 +134,7 @@ void launch_preprocess_backward_multi(const float* rows, uint32_t stride, uint32
 // grad2d -> dL/d(attributes), one thread per Gaussian, stored into `out` in the packed input layout
 // (59*n floats, zeros for invisible Gaussians).
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
+                                const uint32_t* counts, float* grad2d, float* out, uint32_t* status,
                                 cudaStream_t s);
 
 // ---- L1 + SSIM loss -----------------------------------------------------------------------------

@@ -251,7 +251,7 @@ __device__ __forceinline__ void write_packed(const float (*tile)[kBwdPitch], flo
 __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const float* __restrict__ rows, uint32_t stride,
                                                                    uint32_t n, const ViewBlock* __restrict__ vb,
                                                                    const uint32_t* __restrict__ counts,
-                                                                   const float* __restrict__ grad2d,
+                                                                   float* __restrict__ grad2d,
                                                                    float* __restrict__ out, uint32_t* status) {
     pdl_wait();
     static_assert(sizeof(ViewBlock) % 16 == 0, "the view block is copied in 16-byte units");
@@ -295,6 +295,9 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
     const bool vis = lt < cnt && s_cnt[lt] != 0u;
     const int any = __syncthreads_or(vis);
     if (any) {
+        // the slice's 2D gradients are in shared memory now (every thread passed the copy's barrier):
+        // clear them in global memory for the next raster backward, which only accumulates
+        for (uint32_t i = lt; i < 9u * cnt; i += kBwdGroup) grad2d[(size_t)9 * g0 + i] = 0.0f;
         if (lt == 0) {
             mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
             for (int r = kRowRest; r < kRows; ++r)
@@ -359,7 +362,13 @@ __global__ void __launch_bounds__(kBwdGroup) k_preprocess_backward_multi(const f
             __syncthreads();  // sv is rewritten per view
             if (lt < 44) reinterpret_cast<uint32_t*>(&sv)[lt] = reinterpret_cast<const uint32_t*>(mv.view[v])[lt];
             __syncthreads();
-            if (seen & (1u << v)) backward_gaussian(sv, mv.grad2d[v] + (size_t)9 * g, R_, W_, []() {});
+            if (seen & (1u << v)) {
+                float* d2 = mv.grad2d[v] + (size_t)9 * g;
+                backward_gaussian(sv, d2, R_, W_, []() {});
+                // cleared for the next raster backward, which only accumulates
+#pragma unroll
+                for (int k = 0; k < 9; ++k) d2[k] = 0.0f;
+            }
         }
     }
     __syncthreads();
@@ -383,7 +392,7 @@ void launch_preprocess_backward_multi(const float* rows, uint32_t stride, uint32
 }
 
 void launch_preprocess_backward(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view,
-                                const uint32_t* counts, const float* grad2d, float* out, uint32_t* status,
+                                const uint32_t* counts, float* grad2d, float* out, uint32_t* status,
                                 cudaStream_t s) {
     if (n == 0) return;
     launch_pdl(k_preprocess_backward, dim3((n + kBwdGroup - 1u) / kBwdGroup), dim3(kBwdGroup), s, rows, stride, n, view,
