@@ -34,7 +34,7 @@
 namespace gs {
 namespace {
 
-template <int TILE, int BATCH>
+template <int TILE, int BATCH, bool LAST>
 __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(const uint32_t* __restrict__ ranges,
                                                         const uint32_t* __restrict__ vals,
                                                         const float4* __restrict__ rec, uint32_t n,
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
                 cg = __fmaf_rn(b.w * alpha, T, cg);
                 cb = __fmaf_rn(c.x * alpha, T, cb);
                 T = testT;
-                last = pos0 + j;
+                if (LAST) last = pos0 + j;
             }
         }
     }
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
         out.rgb[3 * p + 2] = cb;
     }
     if (out.final_t) out.final_t[p] = T;
-    if (out.n_contrib) out.n_contrib[p] = last;
+    if (LAST) out.n_contrib[p] = last;
     if (out.rgba8) {
         const uint32_t r8 = (uint32_t)(fminf(fmaxf(cr, 0.0f), 1.0f) * 255.0f + 0.5f);
         const uint32_t g8 = (uint32_t)(fminf(fmaxf(cg, 0.0f), 1.0f) * 255.0f + 0.5f);
@@ -146,17 +146,30 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
     }
 }
 
+template <int TILE, int BATCH>
+void launch_batch(const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n, const FrameCtl* ctl,
+                  uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y, const RasterOut& out,
+                  const uint32_t* order, cudaStream_t s) {
+    const dim3 grid(tiles_x * tiles_y), block(TILE * TILE);
+    // the contributor count is tracked only when it is written (a differentiable forward): the
+    // plain frame's raster drops its register and update (0.509 -> 0.499 ms per 1M / 1080p frame)
+    if (out.n_contrib)
+        launch_pdl(k_raster<TILE, BATCH, true>, grid, block, s, ranges, vals, rec, n, ctl, width, height, tiles_x, out,
+                   order);
+    else
+        launch_pdl(k_raster<TILE, BATCH, false>, grid, block, s, ranges, vals, rec, n, ctl, width, height, tiles_x, out,
+                   order);
+}
+
 template <int TILE>
 void launch_tile(uint32_t batch, const uint32_t* ranges, const uint32_t* vals, const float4* rec, uint32_t n,
                  const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
                  const RasterOut& out, const uint32_t* order, cudaStream_t s) {
-    const uint32_t grid = tiles_x * tiles_y;
-    constexpr int threads = TILE * TILE;
     switch (batch) {
-        case 32: launch_pdl(k_raster<TILE, 32>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        case 64: launch_pdl(k_raster<TILE, 64>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        case 128: launch_pdl(k_raster<TILE, 128>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
-        default: launch_pdl(k_raster<TILE, 256>, dim3(grid), dim3(threads), s, ranges, vals, rec, n, ctl, width, height, tiles_x, out, order); break;
+        case 32: launch_batch<TILE, 32>(ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s); break;
+        case 64: launch_batch<TILE, 64>(ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s); break;
+        case 128: launch_batch<TILE, 128>(ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s); break;
+        default: launch_batch<TILE, 256>(ranges, vals, rec, n, ctl, width, height, tiles_x, tiles_y, out, order, s); break;
     }
 }
 
