@@ -302,10 +302,16 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
                      f.vals[0].p, ctl, f.flags.p, 0, s);
     if (profile) cudaEventRecord(ctx->ev[2], s);
     int cur = 0;
+    const uint32_t key_bits = 16u + bitlen(a.tiles_x * a.tiles_y - 1u);
     for (uint32_t p = 0; p < a.passes; ++p) {
+        // the tile digits arrive in depth order, nearly all distinct within a warp: their ranking
+        // matches the high half of the digit and separates the low half by ballots (w/2 of a w-bit
+        // digit, from 2 bits up); the depth digits keep the plain match
+        const uint32_t w = std::min(bits, key_bits - p * bits);
+        const uint32_t split = p * bits >= 16u && w / 2u >= 2u ? w / 2u : 0u;
         launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
                         0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
-                        ctx->cfg.sort_block);
+                        ctx->cfg.sort_block, split);
         cur ^= 1;
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);

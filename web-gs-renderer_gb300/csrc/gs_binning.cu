@@ -367,13 +367,19 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 //   - keys load warp-striped (item k of lane l of warp w is element w*32*ITEMS + k*32 + l), so every
 //     load is a 128-byte line and the warp processes its elements in index order;
 //   - __match_any_sync groups the lanes holding the same digit; a lane's rank is the count of
-//     equal digits in earlier items of its warp plus its rank among the equal lanes (stable);
+//     equal digits in earlier items of its warp plus its rank among the equal lanes (stable). The
+//     match costs more the more distinct values the warp holds: with SPLIT > 0 it matches only the
+//     digit's high bits and separates the low SPLIT bits with one ballot each (measured on the
+//     1M / 1080p frame: the tile digits of keys in depth order are nearly all distinct within a
+//     warp, and their two passes take 16 us less per frame with SPLIT = w/2 of a w-bit digit, while
+//     the depth passes, whose warps hold few distinct digits, are fastest with the plain match);
+//   - ranks (< 4096) are kept two per register, which keeps the thread within 64 registers;
 //   - per-digit warp counts are scanned across warps (warp order = index order), the CTA's digit
 //     totals are published as lookback aggregates and the inclusive prefix of every digit is found
 //     by decoupled lookback (one thread per digit);
 //   - keys/values are staged in shared memory in local sorted order and written out at
 //     global_digit_base + rank, which keeps runs of equal digits contiguous in global memory.
-template <int BITS, int ITEMS>
+template <int BITS, int ITEMS, int SPLIT>
 __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __restrict__ keys_in,
                                                            const uint32_t* __restrict__ vals_in,
                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
@@ -422,7 +428,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
         __syncwarp();
 
         uint32_t key[ITEMS];
-        uint16_t rank[ITEMS];
+        uint32_t rank2[ITEMS / 2];  // rank of item k in bits 16*(k&1) of rank2[k/2]
+#pragma unroll
+        for (uint32_t k = 0; k < ITEMS / 2; ++k) rank2[k] = 0u;
         const uint32_t wbase = base + warp * PER_WARP;
 #pragma unroll
         for (uint32_t k = 0; k < ITEMS; ++k) {
@@ -434,13 +442,20 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             const uint32_t idx = wbase + k * 32u + lane;
             const bool ok = idx < n;
             const uint32_t d = ok ? ((key[k] >> shift) & MASK) : RADIX;  // RADIX marks padding
-            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            // the padding marker's high part (RADIX >> SPLIT) differs from every digit's
+            uint32_t peers = __match_any_sync(0xffffffffu, d >> SPLIT);
+#pragma unroll
+            for (int b = 0; b < SPLIT; ++b) {
+                const bool bit = (d >> b) & 1u;
+                const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+                peers &= bit ? bal : ~bal;
+            }
             const uint32_t pre = ok ? s_whist[warp][d] : 0u;
             __syncwarp();
             if (ok) {
                 const uint32_t below = peers & ((1u << lane) - 1u);
                 if (below == 0u) s_whist[warp][d] = pre + __popc(peers);
-                rank[k] = (uint16_t)(pre + __popc(below));
+                rank2[k / 2] |= (pre + __popc(below)) << (16u * (k & 1u));
             }
             __syncwarp();
         }
@@ -511,7 +526,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             const uint32_t idx = wbase + k * 32u + lane;
             if (idx < n) {
                 const uint32_t d = (key[k] >> shift) & MASK;
-                const uint32_t pos = s_whist[warp][d] + rank[k];
+                const uint32_t pos = s_whist[warp][d] + ((rank2[k / 2] >> (16u * (k & 1u))) & 0xFFFFu);
                 s_keys[pos] = key[k];
                 s_vals[pos] = vals_in[idx];
             }
@@ -689,30 +704,44 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
 
 void configure_sort_kernels() {
     // the largest shared-memory carveout lets more onesweep CTAs (up to 44 KB each) share an SM
-    cudaFuncSetAttribute(k_onesweep<4, 8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_onesweep<4, 16>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_onesweep<8, 8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_onesweep<8, 16>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<4, 8, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<4, 16, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 8, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 8, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 8, 3>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 8, 4>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 16, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 16, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 16, 3>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_onesweep<8, 16, 4>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s, uint32_t block) {
+                     int grid_cap, cudaStream_t s, uint32_t block, uint32_t split) {
     const bool small = block == kSortPartitionMin;
     const uint32_t part = small ? kSortPartitionMin : kSortPartition;
     uint32_t parts = (max_n + part - 1u) / part;
     const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 4u;
     if (parts > cap) parts = cap;
     if (parts == 0) parts = 1;
-#define GS_ONESWEEP(B, I)                                                                                      \
-    launch_pdl(k_onesweep<B, I>, dim3(parts), dim3(kSortThreads), s, keys_in, vals_in, keys_out, vals_out, n_dev, \
+#define GS_ONESWEEP(B, I, S)                                                                                      \
+    launch_pdl(k_onesweep<B, I, S>, dim3(parts), dim3(kSortThreads), s, keys_in, vals_in, keys_out, vals_out, n_dev, \
                n_host, shift, dmask, hist, ctl, flags, slot)
-    if (digit_bits == 4) {
-        if (small) GS_ONESWEEP(4, 8); else GS_ONESWEEP(4, 16);
-    } else {
-        if (small) GS_ONESWEEP(8, 8); else GS_ONESWEEP(8, 16);
+#define GS_ONESWEEP_SPLIT(I)                             \
+    switch (split) {                                     \
+        case 2: GS_ONESWEEP(8, I, 2); break;             \
+        case 3: GS_ONESWEEP(8, I, 3); break;             \
+        case 4: GS_ONESWEEP(8, I, 4); break;             \
+        default: GS_ONESWEEP(8, I, 0); break;            \
     }
+    if (digit_bits == 4) {  // 16 digit values at most: the plain match
+        if (small) GS_ONESWEEP(4, 8, 0); else GS_ONESWEEP(4, 16, 0);
+    } else {
+        if (small) GS_ONESWEEP_SPLIT(8) else GS_ONESWEEP_SPLIT(16)
+    }
+#undef GS_ONESWEEP_SPLIT
 #undef GS_ONESWEEP
 }
 

@@ -82,7 +82,7 @@ void configure_sort_kernels();
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s, uint32_t block = kSortPartition);
+                     int grid_cap, cudaStream_t s, uint32_t block = kSortPartition, uint32_t split = 0);
 // Digit histograms of all passes over the low key_bits bits, for a standalone sort.
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);
