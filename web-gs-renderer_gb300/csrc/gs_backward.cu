@@ -88,10 +88,9 @@ __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, ui
 // dC/dalpha_i = T_i c_i - S_i / (1 - alpha_i), S_i being the colour added behind splat i.
 __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4& a, const float4& b,
                                          const float2& c, float g[9]) {
-    if (pos > p.L) return false;
     const float dx = a.x - p.fx, dy = a.y - p.fy;
     const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
-    if (power > 0.0f || power < c.y) return false;
+    if (pos > p.L || power > 0.0f || power < c.y) return false;
     const float G = raster_expf(power);
     const float og = b.y * G;
     const float alpha = fminf(kAlphaClamp, og);

