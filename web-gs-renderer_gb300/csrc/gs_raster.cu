@@ -116,12 +116,11 @@ __global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(co
                 if (done || power > 0.0f || power < c.y) continue;
                 const float4 b = s_b[j];
                 const float alpha = fminf(kAlphaClamp, b.y * raster_expf(power));
-                if (alpha < kEpsilon) continue;
                 const float testT = T * (1.0f - alpha);
-                if (testT < kBlendThreshold) {
-                    done = true;
-                    continue;
-                }
+                const bool faint = alpha < kEpsilon;
+                const bool stop = !faint && testT < kBlendThreshold;
+                done = done || stop;
+                if (faint || stop) continue;
                 cr = __fmaf_rn(b.z * alpha, T, cr);
                 cg = __fmaf_rn(b.w * alpha, T, cg);
                 cb = __fmaf_rn(c.x * alpha, T, cb);
