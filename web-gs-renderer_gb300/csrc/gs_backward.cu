@@ -107,17 +107,19 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
     const float ug = __fmaf_rn(Tb, b.w, -(p.s_g * ria));
     const float ub = __fmaf_rn(Tb, c.x, -(p.s_b * ria));
     const float dalpha = __fmaf_rn(ur, p.dr, __fmaf_rn(ug, p.dg, ub * p.db));
-    if (og <= kAlphaClamp) {
-        // the constant factors of d power / d(px, py, conic) (-1, -1, -1/2, -1, -1/2) are applied
-        // once per splat after the warp reduction (kGradSign)
-        const float gp = dalpha * og;  // dL/dpower
+    {
+        // a clamped alpha passes no gradient to power and opacity (a select, not a branch: 0.585 ->
+        // 0.580 ms per 1M / 1080p backward); the constant factors of d power / d(px, py, conic)
+        // (-1, -1, -1/2, -1, -1/2) are applied once per splat after the warp reduction (kGradSign)
+        const float da = og <= kAlphaClamp ? dalpha : 0.0f;
+        const float gp = da * og;  // dL/dpower
         const float gpdx = gp * dx, gpdy = gp * dy;
         g[0] = __fmaf_rn(gp, __fmaf_rn(a.z, dx, a.w * dy), g[0]);
         g[1] = __fmaf_rn(gp, __fmaf_rn(b.x, dy, a.w * dx), g[1]);
         g[2] = __fmaf_rn(gpdx, dx, g[2]);
         g[3] = __fmaf_rn(gpdx, dy, g[3]);
         g[4] = __fmaf_rn(gpdy, dy, g[4]);
-        g[5] = __fmaf_rn(dalpha, G, g[5]);
+        g[5] = __fmaf_rn(da, G, g[5]);
     }
     p.s_r = __fmaf_rn(w, b.z, p.s_r);
     p.s_g = __fmaf_rn(w, b.w, p.s_g);
