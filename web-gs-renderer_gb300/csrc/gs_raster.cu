@@ -23,7 +23,7 @@
 //    skipping does not change them.
 //
 // Full residency (2048 threads per SM, 32 registers; the few spilled bytes cost less than the lost
-// warps did).
+// warps did), except for the instantiation that also tracks the contributor count (below).
 //
 // CTA i renders tile order[i]: the tiles listed by decreasing range length, so the longest tiles
 // start first instead of forming the tail of the launch (with tiles in index order the clustered
@@ -34,8 +34,14 @@
 namespace gs {
 namespace {
 
+// Residency: 2048 threads per SM (32 registers); the 16x16 instantiation that also tracks the
+// contributor count runs at 1536 (40 registers, no spills): 0.2705 -> 0.2683 ms per 1M / 1080p
+// differentiable frame, while the plain frame is fastest at full residency (0.2621 against 0.2683).
+template <int TILE, bool LAST>
+constexpr int raster_min_blocks() { return LAST && TILE == 16 ? 6 : 2048 / (TILE * TILE); }
+
 template <int TILE, int BATCH, bool LAST>
-__global__ void __launch_bounds__(TILE * TILE, 2048 / (TILE * TILE)) k_raster(const uint32_t* __restrict__ ranges,
+__global__ void __launch_bounds__(TILE * TILE, raster_min_blocks<TILE, LAST>()) k_raster(const uint32_t* __restrict__ ranges,
                                                         const uint32_t* __restrict__ vals,
                                                         const float4* __restrict__ rec, uint32_t n,
                                                         const FrameCtl* __restrict__ ctl, uint32_t width,
