@@ -66,6 +66,20 @@ def test_odd_image_sizes(gpu_ctx, w, h):
     assert_frame_parity(g, o)
 
 
+@pytest.mark.parametrize("w,h", [(640, 480), (1280, 720), (2048, 1152), (3200, 1800)])
+def test_tile_digit_widths(gpu_ctx, w, h):
+    """The tile passes rank by matching the high half of a w-bit digit and separating the low w/2 bits
+    by ballots (w/2 >= 2): the last tile digit is 3 bits wide here at 640x480 (1200 tiles, plain
+    match), 4 at 1280x720 (split 2), 6 at 2048x1152 and 7 at 3200x1800 (split 3); the first tile digit
+    takes split 4 throughout. Keys, values and pixels bit-exact against the oracle."""
+    spec = W.SceneSpec(60_000, 13, 1, 16, 8.0)
+    packed = spec.build()
+    view = W.CameraSpec((0.0, 0.5, -5.0), (0.0, 0.0, 0.0), 70.0, w, h).view()
+    g, o = _run(gpu_ctx, packed, spec.count, view)
+    assert o["sorted_count"] > 100_000
+    assert_frame_parity(g, o)
+
+
 @pytest.mark.parametrize("count", [0, 1, 2, 33, 2047, 2048, 2049, 4097])
 def test_counts_across_partition_edges(gpu_ctx, count):
     packed = W.SceneSpec(count, 7, 0).build() if count else np.zeros(0, np.float32)
