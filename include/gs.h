@@ -213,6 +213,13 @@ int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, 
  * GS_ERR_TIMEOUT and the context stays usable. */
 int gs_check_wait_timeout(gs_ctx* ctx);
 
+/* Test hook (no counterpart in the reference): sets the sequence number of every frame control block
+ * of ctx -- or, with ctx NULL, of gs_exclusive_scan_static's scratch on the current device. Lookback
+ * words carry the low 30 bits of that number, which advances by 16 per frame or scan, so their tags
+ * repeat every 2^26 calls; the call on which they start again at zero clears the words first. With
+ * this hook a test reaches that call without running 2^26 frames. Synchronous. */
+int gs_debug_set_sequence(gs_ctx* ctx, uint32_t seq);
+
 /* The pinned fp32 exp of the kernels, evaluated on the device (y = exp(x)). */
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
 
@@ -223,10 +230,11 @@ int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t locati
  * forbid a library from allocating behind them. d_in, d_out (n entries; may be the same buffer) and
  * d_total (one entry, or NULL) are device buffers of the current device; work is ordered on
  * `stream` (a cudaStream_t) and the call returns once it has finished. Scratch is a fixed device
- * array of about 74 KB per GPU, held until the process exits; n above 2^24 (16,777,216) returns
- * GS_ERR_INVALID. The first call on a device looks up and clears that array, so make it before any
- * stream capture. All calls share the array: calls that overlap on the GPU (other threads, other
- * streams) race and must be serialised by the caller. */
+ * array of about 74 KB per GPU, zero-filled when the library's device code loads and held until the
+ * process exits; n above 2^24 (16,777,216) returns GS_ERR_INVALID. Every call looks up the array's
+ * device address (no allocation); the first call on a device also loads the library's device code,
+ * so make it before any stream capture. All calls share the array: calls that overlap on the GPU
+ * (other threads, other streams) race and must be serialised by the caller. */
 int gs_exclusive_scan_static(const uint32_t* d_in, uint32_t* d_out, uint32_t n, uint32_t* d_total, void* stream);
 
 /* ---- host utilities (no GPU needed) ----------------------------------------------------------- */

@@ -293,7 +293,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     FrameCtl* ctl = f.ctl.p;
     if (profile) cudaEventRecord(ctx->ev[0], s);
     if (!preprocessed) {
-        launch_frame_begin(ctl, s, f.ranges.p, a.tiles_x * a.tiles_y * 2u);
+        launch_frame_begin(ctl, f.flags.p, (uint32_t)f.flags.cap, s, f.ranges.p, a.tiles_x * a.tiles_y * 2u);
         launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p,
                           f.counts.p, ctl, s);
     }
@@ -393,6 +393,8 @@ int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, con
                         mv.ctl[v] = f.ctl.p;
                         mv.ranges[v] = f.ranges.p;
                         mv.range_words[v] = args[j].tiles_x * args[j].tiles_y * 2u;
+                        mv.flags[v] = f.flags.p;
+                        mv.flag_words[v] = (uint32_t)f.flags.cap;
                         group_of[j] = groups;
                     }
                     cudaStream_t gs = ctx->side[members[c0] % used];
@@ -1150,7 +1152,7 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
     GS_CK(cudaMemcpyAsync(k0, keys, (size_t)n * 4, kin, ctx->stream));
     GS_CK(cudaMemcpyAsync(v0, vals, (size_t)n * 4, kin, ctx->stream));
     FrameCtl* ctl = ctx->aux_ctl.p;
-    launch_frame_begin(ctl, ctx->stream);
+    launch_frame_begin(ctl, ctx->aux_flags.p, (uint32_t)ctx->aux_flags.cap, ctx->stream);
     launch_digit_hist(k0, n, bits, key_bits, ctl->hist, ctx->stream);
     uint32_t* kb[2] = {k0, k1};
     uint32_t* vb[2] = {v0, v1};
@@ -1186,7 +1188,7 @@ int gs_exclusive_scan(gs_ctx* ctx, uint32_t* data, uint32_t n, uint32_t* total, 
     const cudaMemcpyKind kin = location == GS_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     if (n) GS_CK(cudaMemcpyAsync(d, data, (size_t)n * 4, kin, ctx->stream));
     FrameCtl* ctl = ctx->aux_ctl.p;
-    launch_frame_begin(ctl, ctx->stream);
+    launch_frame_begin(ctl, ctx->aux_flags.p, (uint32_t)ctx->aux_flags.cap, ctx->stream);
     GS_CK(cudaMemsetAsync(d + n, 0, 4, ctx->stream));
     launch_exclusive_scan(d, n, d + n, ctl, ctx->aux_flags.p, 0, ctx->stream);
     GS_CK(cudaGetLastError());
@@ -1214,7 +1216,7 @@ int gs_check_wait_timeout(gs_ctx* ctx) {
     }
     GS_CK(cudaMemsetAsync(ctx->aux_u32.p, 0, ((size_t)n + 1) * 4, ctx->stream));
     FrameCtl* ctl = ctx->aux_ctl.p;
-    launch_frame_begin(ctl, ctx->stream);
+    launch_frame_begin(ctl, ctx->aux_flags.p, (uint32_t)ctx->aux_flags.cap, ctx->stream);
     static const uint32_t kOne = 1u;
     GS_CK(cudaMemcpyAsync(&ctl->tickets[0], &kOne, sizeof(kOne), cudaMemcpyHostToDevice, ctx->stream));
     launch_exclusive_scan(ctx->aux_u32.p, n, ctx->aux_u32.p + n, ctl, ctx->aux_flags.p, 0, ctx->stream, 1);
@@ -1222,6 +1224,17 @@ int gs_check_wait_timeout(gs_ctx* ctx) {
     GS_CK(cudaMemcpyAsync(ctx->h_aux, ctl, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
     return status_to_code(ctx, ctx->h_aux->status);
+}
+
+int gs_debug_set_sequence(gs_ctx* ctx, uint32_t seq) {
+    if (!ctx) return static_scan_set_sequence(seq) == cudaSuccess ? GS_OK : GS_ERR_CUDA;
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    std::vector<FrameCtl*> ctls = {ctx->main.ctl.p, ctx->aux_ctl.p};
+    for (Frame* f : ctx->batch) ctls.push_back(f->ctl.p);
+    for (FrameCtl* c : ctls)
+        if (c) GS_CK(cudaMemcpy(&c->seq, &seq, sizeof(seq), cudaMemcpyHostToDevice));
+    return GS_OK;
 }
 
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {

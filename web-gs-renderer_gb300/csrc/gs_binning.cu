@@ -76,16 +76,24 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
 
 // Resets one frame's control block (CTA 0) and clears its tile ranges (renderer.js:919) with
 // 16-byte stores across the CTAs [0, ncta), the tail word by word.
-__device__ __forceinline__ void frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words, uint32_t cta,
-                                            uint32_t ncta) {
+//
+// Lookback words carry only the low 30 bits of the sequence number, which advances by 16 per frame,
+// so the tags repeat every 2^26 frames: a word left from 2^26 frames earlier with a set flag would
+// read as published by the current frame. On the frame whose tags start again at zero, CTA 0 clears
+// the frame's lookback words (`flags`, flag_words words) before any later kernel of the frame can
+// read them. That is one clear every 2^26 frames, on the device, so replayed graphs are covered too.
+__device__ __forceinline__ void frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words, uint64_t* flags,
+                                            uint32_t flag_words, uint32_t cta, uint32_t ncta) {
     const uint32_t t = threadIdx.x;
     const uint32_t quads = range_words / 4u;
     for (uint32_t q = cta * blockDim.x + t; q < quads; q += ncta * blockDim.x)
         reinterpret_cast<uint4*>(ranges)[q] = make_uint4(0u, 0u, 0u, 0u);
     if (cta != 0) return;
     for (uint32_t i = quads * 4u + t; i < range_words; i += blockDim.x) ranges[i] = 0u;
+    const uint32_t next = (ctl->seq & ~15u) + 16u;
+    __syncthreads();  // every thread has read the old sequence number before thread 0 replaces it
     if (t == 0) {
-        ctl->seq = (ctl->seq & ~15u) + 16u;
+        ctl->seq = next;
         ctl->status = 0u;
         ctl->instance_count = 0u;
         ctl->sorted_count = 0u;
@@ -94,17 +102,20 @@ __device__ __forceinline__ void frame_begin(FrameCtl* ctl, uint32_t* ranges, uin
     }
     if (t < 15) ctl->tickets[t] = 0u;
     for (uint32_t i = t; i < 8u * 256u; i += blockDim.x) ctl->hist[i] = 0u;
+    if ((next & kSeqMask) == 0u && flags)
+        for (uint32_t i = t; i < flag_words; i += blockDim.x) flags[i] = 0ull;
 }
 
-__global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words) {
+__global__ void k_frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words, uint64_t* flags,
+                              uint32_t flag_words) {
     pdl_wait();
-    frame_begin(ctl, ranges, range_words, blockIdx.x, gridDim.x);
+    frame_begin(ctl, ranges, range_words, flags, flag_words, blockIdx.x, gridDim.x);
 }
 
 __global__ void k_frame_begin_multi(MultiViewFrames mv) {
     pdl_wait();
     const uint32_t v = blockIdx.y;
-    frame_begin(mv.ctl[v], mv.ranges[v], mv.range_words[v], blockIdx.x, gridDim.x);
+    frame_begin(mv.ctl[v], mv.ranges[v], mv.range_words[v], mv.flags[v], mv.flag_words[v], blockIdx.x, gridDim.x);
 }
 
 // ---- fused offset scan + emit ---------------------------------------------------------------
@@ -672,11 +683,12 @@ void launch_frame_begin_multi(const MultiViewFrames& mv, cudaStream_t s) {
     launch_pdl(k_frame_begin_multi, dim3(grid, mv.count), dim3(256), s, mv);
 }
 
-void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges, uint32_t range_words) {
+void launch_frame_begin(FrameCtl* ctl, uint64_t* flags, uint32_t flag_words, cudaStream_t s, uint32_t* ranges,
+                        uint32_t range_words) {
     // ranges come from cudaMalloc (16-byte aligned); one 16-byte store per thread, up to 64 CTAs
     const uint32_t quads = range_words / 4u;
     const uint32_t grid = std::max(1u, std::min(64u, (quads + 255u) / 256u));
-    launch_pdl(k_frame_begin, dim3(grid), dim3(256), s, ctl, ranges, range_words);
+    launch_pdl(k_frame_begin, dim3(grid), dim3(256), s, ctl, ranges, range_words, flags, flag_words);
 }
 
 void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uint32_t tiles_x, uint32_t max_instance,

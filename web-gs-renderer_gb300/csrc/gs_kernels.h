@@ -40,7 +40,10 @@ inline void launch_pdl(void (*k)(Params...), dim3 grid, dim3 block, cudaStream_t
 
 // ---- frame ----------------------------------------------------------------------------------
 // Resets the frame control block and, when given, clears the frame's tile ranges (range_words words).
-void launch_frame_begin(FrameCtl* ctl, cudaStream_t s, uint32_t* ranges = nullptr, uint32_t range_words = 0);
+// flags / flag_words: every lookback word the kernels of this control block use; they are cleared on
+// the one frame in 2^26 where the words' 30-bit sequence tags start again at zero.
+void launch_frame_begin(FrameCtl* ctl, uint64_t* flags, uint32_t flag_words, cudaStream_t s,
+                        uint32_t* ranges = nullptr, uint32_t range_words = 0);
 
 // Up to kMaxMultiViews views of one scene for launch_preprocess_multi: each view's block and frame
 // outputs.
@@ -53,6 +56,8 @@ struct MultiViewFrames {
     FrameCtl* ctl[kMaxMultiViews];
     uint32_t* ranges[kMaxMultiViews];  // tile ranges, cleared by launch_frame_begin_multi
     uint32_t range_words[kMaxMultiViews];
+    uint64_t* flags[kMaxMultiViews];   // lookback words of each view's frame (see launch_frame_begin)
+    uint32_t flag_words[kMaxMultiViews];
     uint32_t count;
 };
 // launch_frame_begin for every view of mv in one launch (one row of CTAs per view).
@@ -110,6 +115,9 @@ void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const 
                    uint32_t tiles_y, const RasterOut& out, const uint32_t* order, cudaStream_t s);
 
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
+
+// Sets the sequence number of gs_exclusive_scan_static's scratch on the current device (a test hook).
+cudaError_t static_scan_set_sequence(uint32_t seq);
 
 // ---- backward ---------------------------------------------------------------------------------
 // grad2d: 9 floats per Gaussian, dL/d(pixel.x, pixel.y, conic.x, conic.y, conic.z, opacity, r, g, b),

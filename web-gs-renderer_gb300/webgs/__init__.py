@@ -324,6 +324,10 @@ class Context:
         self._ck(library().gs_exclusive_scan(self.handle, _ptr(d), d.size, C.byref(tot), GS_MEM_HOST))
         return d, tot.value
 
+    def set_sequence(self, seq: int) -> None:
+        """Test hook: sets the lookback sequence number of every frame control block of the context."""
+        self._ck(library().gs_debug_set_sequence(self.handle, seq & 0xFFFFFFFF))
+
     def exp(self, x: np.ndarray) -> np.ndarray:
         xx = np.ascontiguousarray(x, dtype=np.float32)
         y = np.empty_like(xx)

@@ -115,6 +115,7 @@ SIGNATURES = [
     ("gs_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
     ("gs_check_wait_timeout", C.c_int, [C.c_void_p]),
     ("gs_exclusive_scan_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("gs_debug_set_sequence", C.c_int, [C.c_void_p, C.c_uint32]),
     ("gs_camera_view", C.c_int, [C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
                                  C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.POINTER(View)]),
     ("gs_synth_scene", C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]),
