@@ -45,6 +45,8 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--launch-check", action="store_true",
+                    help="start the ranks and report them (gloo, no GPU work, no metric): a check of the launcher")
     return ap.parse_args()
 
 
@@ -174,15 +176,14 @@ def cpu_frame_rate(packed, count, view, target_s: float, row_stride: int = 1, th
 def run_reference(args, rank: int, world: int) -> None:
     if rank != 0:
         return
-    from webgs import workloads as W
+    import oracle
+    from webgs import workloads as W  # the workload's sizes only: no product code is loaded
 
     spec, cam = W.SCENE_1M, W.CAMERA_1080P
-    packed = spec.build()
-    view = cam.view()
-    import oracle
-    import webgs
-
-    vb = webgs.view_bytes(view)
+    # inputs from the oracle's own generators (bit-identical to the product's, tests/test_oracle_inputs.py)
+    packed = oracle.synth_scene(spec.kind, spec.count, spec.seed, spec.clusters, spec.box)
+    vb = oracle.camera_view(cam.eye, cam.target, (0.0, 1.0, 0.0), cam.fovy, cam.width, cam.height, cam.z_near,
+                            cam.z_far)
     threads = os.cpu_count() or 1
     # size the step so W + K steps take about two minutes: the whole frame when that fits, else the
     # global passes plus every m-th tile row of the raster
@@ -235,6 +236,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     dist = None
     if world > 1:
         import torch.distributed as dist  # noqa: F811
+        if torch.cuda.device_count() <= local_rank:
+            raise SystemExit(f"rank {rank}: --gpus {world} needs {world} GPUs, this node has "
+                             f"{torch.cuda.device_count()}")
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     torch.cuda.set_device(local_rank)
@@ -439,12 +443,52 @@ def fwd_bwd(spec, cam, packed, steps, warmup, local_rank) -> dict:
             "workload": f"{n} Gaussians {w}x{h}, L1 + 0.2(1-SSIM) vs perturbed-scene target, grads of 59*N floats"}
 
 
+def launch_ranks(args) -> int:
+    """`bench.py --gpus N` started without a launcher: one process per GPU through
+    torch.distributed.run (rendezvous on 127.0.0.1), the same command line in every rank; rank 0
+    prints the JSON line. Returns the launcher's exit status."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    env = dict(os.environ)
+    # the launcher would pin every rank to one OpenMP thread; the ranks share the host's cores instead
+    env.setdefault("OMP_NUM_THREADS", str(max(1, (os.cpu_count() or 1) // args.gpus)))
+    return subprocess.call(cmd, env=env)
+
+
+def launch_check(rank: int, world: int) -> None:
+    """Every rank joins a gloo group and reports its rank; rank 0 prints them (no GPU, no metric)."""
+    import torch
+    import torch.distributed as dist
+
+    if world > 1:
+        dist.init_process_group("gloo")
+        ranks = [None] * world
+        dist.all_gather_object(ranks, {"rank": rank, "local_rank": int(os.environ.get("LOCAL_RANK", "0")),
+                                       "pid": os.getpid()})
+        dist.barrier()
+        dist.destroy_process_group()
+    else:
+        ranks = [{"rank": 0, "local_rank": 0, "pid": os.getpid()}]
+    if rank == 0:
+        print(json.dumps({"launch_check": True, "n_gpus": world, "ranks": ranks, "torch": torch.__version__}),
+              flush=True)
+
+
 def main():
     args = parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args))
     rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.launch_check:
+        launch_check(rank, world)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local_rank)

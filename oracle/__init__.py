@@ -50,6 +50,11 @@ def load() -> C.CDLL:
         lib.oracle_radix_sort_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]
         lib.oracle_exclusive_scan.restype = C.c_uint32
         lib.oracle_exclusive_scan.argtypes = [C.c_void_p, C.c_uint32]
+        lib.oracle_camera_view.argtypes = [C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
+                                           C.POINTER(C.c_float * 3), C.c_float, C.c_uint32, C.c_uint32, C.c_float,
+                                           C.c_float, C.c_void_p]
+        lib.oracle_synth_scene.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]
+        lib.oracle_perturb_scene.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_float]
         _LIB = lib
     return _LIB
 
@@ -174,3 +179,31 @@ def loss_l1_ssim(x: np.ndarray, y: np.ndarray, lam: float = 0.2, grad: bool = Tr
     g = np.zeros_like(xx) if grad else None
     val = lib.oracle_loss_l1_ssim(xx.ctypes.data, yy.ctypes.data, w, h, lam, g.ctypes.data if grad else None)
     return float(val), g
+
+
+# ---- inputs of the benchmark configurations (gs_inputs.cpp), built without the product library ----
+def camera_view(eye, target, up=(0.0, 1.0, 0.0), fovy_deg: float = 60.0, width: int = 512, height: int = 512,
+                z_near: float = 0.2, z_far: float = 1000.0) -> bytes:
+    """The 176-byte GlobalUniforms block of a camera at `eye` looking at `target` (camera.js:87-98)."""
+    f3 = C.c_float * 3
+    out = C.create_string_buffer(176)
+    rc = load().oracle_camera_view(C.byref(f3(*eye)), C.byref(f3(*target)), C.byref(f3(*up)), fovy_deg, width,
+                                   height, z_near, z_far, out)
+    if rc != 0:
+        raise ValueError("oracle_camera_view: bad camera")
+    return out.raw
+
+
+def synth_scene(kind: int, count: int, seed: int, clusters: int = 0, box: float = 0.0) -> np.ndarray:
+    """Seeded synthetic scene in the packed layout (59*count float32)."""
+    packed = np.empty(59 * count, np.float32)
+    if load().oracle_synth_scene(kind, count, seed, clusters, box, packed.ctypes.data) != 0:
+        raise ValueError("oracle_synth_scene: bad arguments")
+    return packed
+
+
+def perturb_scene(packed: np.ndarray, count: int, seed: int, sigma_mean: float, sigma_sh: float) -> np.ndarray:
+    """A perturbed copy: means + N(0, sigma_mean^2), SH + N(0, sigma_sh^2)."""
+    out = np.array(packed, dtype=np.float32, copy=True)
+    load().oracle_perturb_scene(out.ctypes.data, count, seed, sigma_mean, sigma_sh)
+    return out

@@ -22,6 +22,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "libwebgs.so"
 ORACLE_SRC = ROOT / "oracle" / "gs_oracle.cpp"
+ORACLE_INPUTS = ROOT / "oracle" / "gs_inputs.cpp"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -90,9 +91,9 @@ def build_library(force: bool = False) -> Path:
 def build_oracle(force: bool = False) -> Path:
     """Compiles the CPU restatement used by the tests and the CPU baseline."""
     hdr = ORACLE_SRC.with_suffix(".h")
-    if force or _stale(ORACLE_LIB, [ORACLE_SRC, hdr, Path(__file__)]):
+    if force or _stale(ORACLE_LIB, [ORACLE_SRC, ORACLE_INPUTS, hdr, Path(__file__)]):
         _run(["g++", "-O3", "-shared", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall",
-              str(ORACLE_SRC), "-o", str(ORACLE_LIB)])
+              str(ORACLE_SRC), str(ORACLE_INPUTS), "-o", str(ORACLE_LIB)])
     return ORACLE_LIB
 
 
