@@ -22,8 +22,11 @@ extern "C" {
 #define GS_OK 0
 #define GS_ERR_INVALID 1   /* bad argument: null pointer, size out of range, unknown option */
 #define GS_ERR_OOM 2       /* device or pinned host allocation failed */
-#define GS_ERR_OVERFLOW 3  /* instances exceeded max_instance: output written, truncated exactly as
-                              emit.wgsl:57-59 truncates (a soft error) */
+#define GS_ERR_OVERFLOW 3  /* instances exceeded max_instance: output written (a soft error), the
+                              instances truncated exactly as emit.wgsl:57-59 truncates them; tile
+                              ranges and raster use min(I, max_instance), so the last kept tile
+                              renders, where the reference leaves its end unwritten
+                              (tile_ranges.wgsl:14,32 bound by the unclamped I) */
 #define GS_ERR_TIMEOUT 4   /* a device-side wait hit its iteration limit; results are invalid */
 #define GS_ERR_CUDA 5      /* a CUDA runtime call failed; gs_last_error() has the message */
 #define GS_ERR_STATE 6     /* call out of order, e.g. backward without a matching forward */

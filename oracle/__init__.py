@@ -55,6 +55,8 @@ def load() -> C.CDLL:
                                            C.c_float, C.c_void_p]
         lib.oracle_synth_scene.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]
         lib.oracle_perturb_scene.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_float]
+        lib.oracle_tile_ranges_reference.restype = C.c_uint32
+        lib.oracle_tile_ranges_reference.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
         _LIB = lib
     return _LIB
 
@@ -138,6 +140,15 @@ def exclusive_scan(data: np.ndarray) -> tuple[np.ndarray, int]:
     d = np.array(data, dtype=np.uint32, copy=True)
     tot = load().oracle_exclusive_scan(d.ctypes.data, d.size)
     return d, int(tot)
+
+
+def tile_ranges_reference(keys: np.ndarray, sorted_count: int, instance_count: int, tiles: int) -> tuple[np.ndarray, int]:
+    """tile_ranges.wgsl as the reference binds it (unclamped instance count); returns (ranges,
+    threads that would read past the keys buffer)."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
+    ranges = np.zeros(2 * tiles, np.uint32)
+    beyond = load().oracle_tile_ranges_reference(k.ctypes.data, k.size, sorted_count, instance_count, ranges.ctypes.data)
+    return ranges, int(beyond)
 
 
 def backward_f64(view: bytes, packed: np.ndarray, count: int, dl_drgb: np.ndarray, tile: int = 16, factor: int = 64,

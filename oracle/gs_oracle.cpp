@@ -341,7 +341,7 @@ uint32_t exclusive_scan(uint32_t* data, uint64_t n) {
     return carry;
 }
 
-// emit.wgsl:95-133.
+// emit.wgsl:28-66.
 void emit(const uint32_t* offsets, const uint32_t* meta, uint32_t count, uint32_t tilesPerRow,
           uint32_t maxInstanceCount, uint32_t* keys, uint32_t* vals, int threads) {
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(threads)
@@ -411,6 +411,39 @@ void tile_ranges(const uint32_t* keys, uint32_t n, uint32_t* ranges) {
     }
 }
 
+// tile_ranges.wgsl:7-34 exactly as the reference binds it, for the overflow contract: the pass is
+// dispatched with the sort's indirect grid, ceil(min(I, capacity) / 256) workgroups of 256
+// (indirect_arg.wgsl:16-21), but its bound and its last-instance test use the unclamped instance
+// count I (renderer.js:612 binds instanceCountBuffer, tile_ranges.wgsl:14,32). With I > capacity the
+// last tile's end is never written (it keeps the 0 of renderer.js:919), and threads at or past the
+// capacity would read beyond the keys buffer, which WGSL leaves to the implementation (robust buffer
+// access); they are not restated, only counted (the return value).
+uint32_t tile_ranges_as_bound(const uint32_t* keys, uint32_t capacity, uint32_t sorted, uint32_t instanceCount,
+                              uint32_t* ranges) {
+    const uint64_t threads = ((uint64_t)sorted + 255u) / 256u * 256u;
+    uint32_t beyond = 0;
+    for (uint64_t g = 0; g < threads; ++g) {
+        const uint32_t gindex = (uint32_t)g;
+        if (gindex >= instanceCount) continue;
+        if (gindex >= capacity) {
+            ++beyond;
+            continue;
+        }
+        const uint32_t tileIndex = keys[gindex] >> 16u;
+        if (gindex == 0u) {
+            ranges[tileIndex * 2] = 0u;
+        } else {
+            const uint32_t prev = keys[gindex - 1] >> 16u;
+            if (tileIndex > prev) {
+                ranges[prev * 2 + 1] = gindex;
+                ranges[tileIndex * 2] = gindex;
+            }
+        }
+        if (gindex == instanceCount - 1u) ranges[tileIndex * 2 + 1] = instanceCount;
+    }
+    return beyond;
+}
+
 // raseter.wgsl:35-117. One pixel walks its tile's range front to back. The reference's batches of
 // 256 and its all-done vote only skip work for pixels that are already done, so a per-pixel walk
 // gives the same result.
@@ -441,7 +474,7 @@ void raster(const Uniforms& u, uint32_t tile, const uint32_t* ranges, const uint
                             cc = pre.conic_opacity[4 * (size_t)g + 2], o = pre.conic_opacity[4 * (size_t)g + 3];
                     const T dx = pre.pixel[2 * (size_t)g] - fpx;
                     const T dy = pre.pixel[2 * (size_t)g + 1] - fpy;
-                    // calculatePower :307-311, contracted as pinned (rule 5)
+                    // calculatePower raseter.wgsl:112-116, contracted as pinned (rule 5)
                     const T q = Num<T>::fma(a * dx, dx, (cc * dy) * dy);
                     const T power = Num<T>::fma((T)-0.5f, q, -((b * dx) * dy));
                     if (power > (T)0) continue;
@@ -592,6 +625,11 @@ void oracle_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_
 }
 
 uint32_t oracle_exclusive_scan(uint32_t* data, uint32_t n) { return exclusive_scan(data, n); }
+
+uint32_t oracle_tile_ranges_reference(const uint32_t* keys, uint32_t capacity, uint32_t sorted,
+                                      uint32_t instance_count, uint32_t* ranges) {
+    return tile_ranges_as_bound(keys, capacity, sorted, instance_count, ranges);
+}
 
 }  // extern "C"
 

@@ -92,6 +92,14 @@ void oracle_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, uint32_
  * the total. */
 uint32_t oracle_exclusive_scan(uint32_t* data, uint32_t n);
 
+/* tile_ranges.wgsl:7-34 as the reference binds it (renderer.js:612): dispatched over ceil(sorted/256)
+ * workgroups of 256 but bounded by the unclamped instance count. keys holds `capacity` sorted keys
+ * (the first `sorted` valid); ranges (2T words) must be zeroed first. When instance_count exceeds
+ * the capacity the last tile's end stays 0. Returns how many threads would read past the keys
+ * buffer (left undefined by WGSL, not restated); 0 whenever sorted is a multiple of 256. */
+uint32_t oracle_tile_ranges_reference(const uint32_t* keys, uint32_t capacity, uint32_t sorted,
+                                      uint32_t instance_count, uint32_t* ranges);
+
 #ifdef __cplusplus
 }
 #endif

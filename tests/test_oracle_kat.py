@@ -93,7 +93,7 @@ def test_equal_depth_ties_sort_by_gaussian_index():
 def test_saturating_stack_stops_before_the_saturating_splat():
     # eight opaque splats at the same spot, front to back; alpha clamps at 0.99. In fp32,
     # T after one splat is 1 - 0.99f = 0.00999999, and the second splat's testT = 9.99998e-5 is below
-    # the f32 threshold 1e-4 (1.00000005e-4): the pixel ends without blending it (raseter.wgsl:287-291)
+    # the f32 threshold 1e-4 (1.00000005e-4): the pixel ends without blending it (raseter.wgsl:91-95)
     z = [0.0 + 0.01 * k for k in range(8)]
     packed, n = packed_scene([[0, 0, zz] for zz in z], [[0.0] * 3] * 8, [[1, 0, 0, 0]] * 8, [[1, 1, 1]] * 8,
                              [20.0] * 8)
@@ -123,6 +123,31 @@ def test_overflow_truncates_at_max_instance():
     assert set(np.unique(trunc["vals"]).tolist()) == set(first.tolist())
     starts, ends = trunc["ranges"][0::2], trunc["ranges"][1::2]
     assert ends.max() == 300 and np.all(ends >= starts)
+
+
+def test_overflow_tile_ranges_differ_from_reference_only_at_the_last_tile():
+    """The deliberate deviation of the overflow contract. With I > max_instance the reference's tile
+    ranges pass is bounded by the unclamped count I (renderer.js:612, tile_ranges.wgsl:14,32), so the
+    last kept tile's end is never written and that tile rasterizes nothing; this pipeline bounds the
+    pass by min(I, max_instance) and closes the last tile at max_instance. Every other range agrees.
+    256 slots fill the indirect grid exactly, so no reference thread reads past the keys."""
+    packed = webgs.synth_scene(0, 256, 4)
+    trunc = run(camera(), packed, 256, factor=1)
+    I, cap = trunc["instance_count"], trunc["sorted_count"]
+    assert I > cap == 256
+    tiles = trunc["tiles_x"] * trunc["tiles_y"]
+    ref, beyond = oracle.tile_ranges_reference(trunc["keys"], cap, I, tiles)
+    assert beyond == 0
+    last = int(trunc["keys"][cap - 1] >> 16)
+    ours = trunc["ranges"].copy()
+    assert ours[2 * last + 1] == cap and ref[2 * last + 1] == 0 and ref[2 * last] == ours[2 * last] > 0
+    ours[2 * last + 1] = 0
+    np.testing.assert_array_equal(ref, ours)
+    # without overflow both bounds are the same count and the ranges agree everywhere
+    full = run(camera(), packed, 256)
+    ref_full, beyond = oracle.tile_ranges_reference(full["keys"], full["sorted_count"], full["instance_count"], tiles)
+    assert beyond == 0
+    np.testing.assert_array_equal(ref_full, full["ranges"])
 
 
 def test_scan_restatement_is_exclusive_prefix_sum():

@@ -455,7 +455,7 @@ void gs_config_default(gs_config* cfg) {
     if (!cfg) return;
     cfg->tile_size = 16;            // TILE_SIZE_X/Y, renderer.js:25-26
     cfg->digit_bits = 8;            // RADIX_DIGITS = 256, renderer.js:67
-    cfg->raster_batch = 256;        // TIlE_SIZE batch, raseter.wgsl:217
+    cfg->raster_batch = 256;        // TIlE_SIZE batch, raseter.wgsl:21-23
     cfg->max_instance_factor = 64;  // MAX_INSTANCE_FACTOR, renderer.js:16
     cfg->flags = 0;
     cfg->device = 0;

@@ -232,7 +232,7 @@ const PlyType kPlyTypes[] = {
     {"float", 4, 2},  {"float32", 4, 2}, {"double", 8, 3}, {"float64", 8, 3},
 };
 
-// loader.js:3-11: the 59 properties, in the order of the packed layout (loader.js:246-270)
+// loader.js:3-11: the 59 properties, in the order of the packed layout (loader.js:75-110, 143-147)
 std::vector<std::string> required_properties() {
     std::vector<std::string> r = {"x", "y", "z", "scale_0", "scale_1", "scale_2", "rot_0", "rot_1", "rot_2", "rot_3",
                                   "f_dc_0", "f_dc_1", "f_dc_2", "opacity"};
@@ -270,7 +270,7 @@ int ply_fail(char* err, size_t err_len, const std::string& msg) {
 extern "C" int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, float* packed, char* err,
                             size_t err_len) {
     if (!bytes || !count) return ply_fail(err, err_len, "Invalid PLY: null buffer");
-    // findHeaderEnd (loader.js:277-295): "end_header", then an optional "\r" and an optional "\n"
+    // findHeaderEnd (loader.js:118-136): "end_header", then an optional "\r" and an optional "\n"
     static const char kEnd[] = "end_header";
     const size_t kEndLen = sizeof(kEnd) - 1;
     size_t idx = size;
@@ -280,7 +280,7 @@ extern "C" int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, 
     size_t body = idx + kEndLen;
     if (body < size && bytes[body] == '\r') ++body;
     if (body < size && bytes[body] == '\n') ++body;
-    // parseHeader (loader.js:310-373)
+    // parseHeader (loader.js:151-213)
     std::string header(reinterpret_cast<const char*>(bytes), body);
     long long vcount = 0;
     bool little = false, has_format = false;
@@ -340,7 +340,7 @@ extern "C" int gs_ply_parse(const uint8_t* bytes, size_t size, uint32_t* count, 
     if (body + n * stride > size) return ply_fail(err, err_len, "Invalid PLY: vertex data truncated");
     *count = (uint32_t)n;
     if (!packed) return GS_OK;
-    // loader.js:246-270: positions, scales, rotations, f_dc, opacity, f_rest blocks
+    // loader.js:80-110, 143-147: positions, scales, rotations, f_dc, opacity, f_rest blocks
     const uint64_t width[6] = {3, 3, 4, 3, 1, 45};
     uint64_t base[6];
     base[0] = 0;

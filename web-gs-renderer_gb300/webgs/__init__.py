@@ -24,7 +24,7 @@ __all__ = [
     "GS_FLAG_DIFFERENTIABLE", "GS_MEM_HOST", "GS_MEM_DEVICE", "library",
 ]
 
-FLOATS_PER_GAUSSIAN = 59  # 3 pos + 3 scale + 4 rot + 3 dc + 1 opacity + 45 rest (loader.js:236)
+FLOATS_PER_GAUSSIAN = 59  # 3 pos + 3 scale + 4 rot + 3 dc + 1 opacity + 45 rest (loader.js:77)
 
 
 class GsError(RuntimeError):
