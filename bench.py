@@ -45,6 +45,9 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="time the CPU oracle on every benchmark configuration (all host cores and one core) "
+                         "and print one JSON line; no GPU work")
     ap.add_argument("--launch-check", action="store_true",
                     help="start the ranks and report them (gloo, no GPU work, no metric): a check of the launcher")
     return ap.parse_args()
@@ -171,6 +174,92 @@ def cpu_frame_rate(packed, count, view, target_s: float, row_stride: int = 1, th
     mean = sum(times) / len(times)
     return {"value": pix / mean / 1e6, "ms_per_frame": mean * 1e3, "frames": frames, "threads": threads,
             "pixels_per_frame": pix}
+
+
+def _cpu_inputs(spec, cam):
+    """The scene and the view block from the oracle's own generators (no product library)."""
+    import oracle
+
+    packed = oracle.synth_scene(spec.kind, spec.count, spec.seed, spec.clusters, spec.box)
+    vb = oracle.camera_view(cam.eye, cam.target, (0.0, 1.0, 0.0), cam.fovy, cam.width, cam.height, cam.z_near,
+                            cam.z_far)
+    return packed, vb
+
+
+def cpu_forward(vb: bytes, packed, n: int, threads: int) -> dict:
+    """One fp32 frame of the oracle: wall ms and per-pass ms."""
+    import oracle
+
+    t0 = time.perf_counter()
+    o = oracle.forward_f32(vb, packed, n, threads=threads, keys=False, timed=True)
+    ms = (time.perf_counter() - t0) * 1e3
+    return {"ms": round(ms, 2), "passes_ms": {k: round(v, 2) for k, v in o["pass_ms"].items()}, "rgb": o["rgb"]}
+
+
+def cpu_forward_backward(vb: bytes, packed, n: int, target, threads: int) -> dict:
+    """One differentiation step on the CPU: the fp32 frame, the FP64 L1 + 0.2 (1 - SSIM) loss and its
+    image gradient, and the FP64 adjoint of the whole pipeline (which re-runs the frame in FP64)."""
+    import oracle
+
+    f = cpu_forward(vb, packed, n, threads)
+    t0 = time.perf_counter()
+    _, dl = oracle.loss_l1_ssim(f["rgb"], target, 0.2)
+    t_loss = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    oracle.backward_f64(vb, packed, n, dl, threads=threads)
+    t_bwd = (time.perf_counter() - t0) * 1e3
+    passes = dict(f["passes_ms"])
+    passes.update({"loss (FP64)": round(t_loss, 2), "adjoint backward (FP64)": round(t_bwd, 2)})
+    return {"ms": round(f["ms"] + t_loss + t_bwd, 2), "passes_ms": passes}
+
+
+def cpu_configs(threads_list) -> dict:
+    """The oracle (oracle/, C++ with OpenMP) on every benchmark configuration, per pass, with each
+    thread count of threads_list; the CPU baselines beside the GPU numbers of each configuration."""
+    import oracle
+    from webgs import workloads as W
+
+    out = {}
+    for threads in threads_list:
+        row = {}
+        packed, vb = _cpu_inputs(W.SMALL_SCENE, W.SMALL_CAMERA)
+        f = cpu_forward(vb, packed, W.SMALL_SCENE.count, threads)
+        row["small 50k 512x512 fwd"] = {"ms_per_frame": f["ms"], "passes_ms": f["passes_ms"],
+                                        "Mpix_s": round(512 * 512 / f["ms"] / 1e3, 3)}
+        packed, vb = _cpu_inputs(W.SCENE_1M, W.CAMERA_1080P)
+        f = cpu_forward(vb, packed, W.SCENE_1M.count, threads)
+        row["scene 1M 1920x1080 fwd"] = {"ms_per_frame": f["ms"], "passes_ms": f["passes_ms"],
+                                         "Mpix_s": round(1920 * 1080 / f["ms"] / 1e3, 3)}
+        spec, cam = W.SCENE_500K, W.CAMERA_720P
+        packed, vb = _cpu_inputs(spec, cam)
+        target = oracle.forward_f32(vb, oracle.perturb_scene(packed, spec.count, 99, 0.01, 0.02), spec.count,
+                                    threads=threads, keys=False)["rgb"]
+        fb = cpu_forward_backward(vb, packed, spec.count, target, threads)
+        row["diff 500k 1280x720 fwd+bwd"] = {"ms_per_step": fb["ms"], "passes_ms": fb["passes_ms"],
+                                             "Mpix_s": round(1280 * 720 / fb["ms"] / 1e3, 3)}
+        # batched forward: the 16 orbit views of the three scenes (one core: the first four views)
+        packs = [oracle.synth_scene(sp.kind, sp.count, sp.seed, sp.clusters, sp.box) for sp in W.BATCH_SCENES]
+        cams = W.orbit_cameras(16, 2024, 9.0)
+        sample = cams if threads > 1 else cams[:4]
+        ms, pix = 0.0, 0
+        for si, c in sample:
+            vbv = oracle.camera_view(c.eye, c.target, (0.0, 1.0, 0.0), c.fovy, c.width, c.height, c.z_near, c.z_far)
+            ms += cpu_forward(vbv, packs[si], W.BATCH_SCENES[si].count, threads)["ms"]
+            pix += c.width * c.height
+        row["batched 16 views fwd"] = {"ms_per_view": round(ms / len(sample), 2), "Mpix_s": round(pix / ms / 1e3, 3),
+                                       "views_timed": len(sample)}
+        # batched forward+backward: 3M scene, 8 views at 1080p (timed: the first view)
+        spec = W.SCENE_3M
+        packed = oracle.synth_scene(spec.kind, spec.count, spec.seed, spec.clusters, spec.box)
+        c = [c for _, c in W.orbit_cameras(8, 77, 18.0, fixed_resolution=(1920, 1080))][0]
+        vbv = oracle.camera_view(c.eye, c.target, (0.0, 1.0, 0.0), c.fovy, c.width, c.height, c.z_near, c.z_far)
+        target = oracle.forward_f32(vbv, oracle.perturb_scene(packed, spec.count, 99, 0.01, 0.02), spec.count,
+                                    threads=threads, keys=False)["rgb"]
+        fb = cpu_forward_backward(vbv, packed, spec.count, target, threads)
+        row["batched 3M 8x1080p fwd+bwd"] = {"ms_per_view": fb["ms"], "passes_ms": fb["passes_ms"],
+                                             "views_timed": 1}
+        out[f"{threads}_threads"] = row
+    return out
 
 
 def run_reference(args, rank: int, world: int) -> None:
@@ -316,10 +405,12 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     # all 59 attributes, everything on the device; timed like the forward
     scene.close()
     ctx.close()
+    cpu_legs = not args.no_cpu_baseline and world == 1
     fb_1080 = fwd_bwd(W.SCENE_1M, W.CAMERA_1080P, packed, args.steps, args.warmup, local_rank)
-    fb_720 = fwd_bwd(W.SCENE_500K, W.CAMERA_720P, None, args.steps, args.warmup, local_rank)
-    batched = None if args.no_batched else batched_forward(args.steps, args.warmup, local_rank)
-    batched_fb = None if args.no_batched else batched_fwd_bwd(max(3, args.steps // 5), args.warmup, local_rank)
+    fb_720 = fwd_bwd(W.SCENE_500K, W.CAMERA_720P, None, args.steps, args.warmup, local_rank, cpu=cpu_legs)
+    batched = None if args.no_batched else batched_forward(args.steps, args.warmup, local_rank, cpu=cpu_legs)
+    batched_fb = (None if args.no_batched else
+                  batched_fwd_bwd(max(3, args.steps // 5), args.warmup, local_rank, cpu=cpu_legs))
 
     if rank != 0:
         if dist:
@@ -372,7 +463,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         dist.destroy_process_group()
 
 
-def fwd_bwd(spec, cam, packed, steps, warmup, local_rank) -> dict:
+def fwd_bwd(spec, cam, packed, steps, warmup, local_rank, cpu: bool = False) -> dict:
     """ms per forward + loss + backward step on the device (CUDA events on the context stream)."""
     import ctypes as C
 
@@ -438,9 +529,21 @@ def fwd_bwd(spec, cam, packed, steps, warmup, local_rank) -> dict:
                 acc[k] = acc.get(k, 0.0) + v["ms"] / prof_steps
     psc.close()
     pctx.close()
-    return {"ms_per_step": round(ms, 4), "Mpix/s": round(w * h / ms / 1e3, 2), "loss": round(loss.value, 6),
-            "passes_ms": {k: round(v, 4) for k, v in acc.items()},
-            "workload": f"{n} Gaussians {w}x{h}, L1 + 0.2(1-SSIM) vs perturbed-scene target, grads of 59*N floats"}
+    res = {"ms_per_step": round(ms, 4), "Mpix/s": round(w * h / ms / 1e3, 2), "loss": round(loss.value, 6),
+           "passes_ms": {k: round(v, 4) for k, v in acc.items()},
+           "workload": f"{n} Gaussians {w}x{h}, L1 + 0.2(1-SSIM) vs perturbed-scene target, grads of 59*N floats"}
+    if cpu:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        vb = webgs.view_bytes(view)
+        target_cpu = oracle.forward_f32(vb, webgs.perturb_scene(packed, n, 99, 0.01, 0.02), n, threads=threads,
+                                        keys=False)["rgb"]
+        c = cpu_forward_backward(vb, packed, n, target_cpu, threads)
+        res["cpu_baseline"] = {"value": round(w * h / c["ms"] / 1e3, 4), "unit": "Mpix/s", "ms_per_step": c["ms"],
+                               "cores": threads, "kind": "port", "passes_ms": c["passes_ms"],
+                               "sample": "one step of the same workload: fp32 frame, FP64 loss, FP64 adjoint"}
+    return res
 
 
 def launch_ranks(args) -> int:
@@ -488,6 +591,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.launch_check:
         launch_check(rank, world)
+    elif args.cpu_configs:
+        if rank == 0:
+            cores = os.cpu_count() or 1
+            print(json.dumps({"cpu_configs": cpu_configs([cores, 1]), "cores": cores, "kind": "port",
+                              "note": "the oracle (oracle/, C++/OpenMP): fp32 frames, FP64 loss and FP64 adjoint"}),
+                  flush=True)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
@@ -509,7 +618,7 @@ def _timed(stream, fn, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def batched_forward(steps, warmup, local_rank) -> dict:
+def batched_forward(steps, warmup, local_rank, cpu: bool = False) -> dict:
     """3 scenes (100k, 400k, 1.5M; seeds 3-5), 16 cameras on random orbits, resolutions from
     {640x480, 1280x720, 1920x1080}: one batched launch vs 16 plain frames. The autotuner first picks
     tile size, digit width, raster batch depth and sort block on the whole batch."""
@@ -620,10 +729,18 @@ def batched_forward(steps, warmup, local_rank) -> dict:
             s.close()
         ctx.close()
     res["autotune"] = {"best": tuned, "best_ms_per_batch": round(tuned_ms, 4), "sweep_s": round(tune_s, 1)}
+    if cpu:
+        threads = os.cpu_count() or 1
+        ms = sum(cpu_forward(webgs.view_bytes(v), packs[si], W.BATCH_SCENES[si].count, threads)["ms"]
+                 for (si, _), v in zip(cams, views))
+        pix = sum(c.width * c.height for _, c in cams)
+        res["cpu_baseline"] = {"value": round(pix / ms / 1e3, 4), "unit": "Mpix/s",
+                               "ms_per_view": round(ms / len(cams), 2), "cores": threads, "kind": "port",
+                               "sample": "every one of the 16 views once, one after another (fp32 frames)"}
     return res
 
 
-def batched_fwd_bwd(steps, warmup, local_rank) -> dict:
+def batched_fwd_bwd(steps, warmup, local_rank, cpu: bool = False) -> dict:
     """One 3M-Gaussian scene (seed 6, 128 clusters, 40^3 box), 8 cameras at 1920x1080: one batched
     forward + 8 losses + one batched backward (gradients of the 8 views summed) vs 8 sequential
     forward + loss + backward calls."""
@@ -683,9 +800,21 @@ def batched_fwd_bwd(steps, warmup, local_rank) -> dict:
     ms_bat = _timed(stream, batched, steps, warmup)
     sc.close()
     ctx.close()
-    return {"workload": "3M Gaussians (128 clusters, 40^3 box, seed 6), 8 x 1920x1080, L1 + 0.2(1-SSIM)",
-            "sequential_ms_per_view": round(ms_seq / len(views), 4), "batched_ms_per_view": round(ms_bat / len(views), 4),
-            "batched_over_sequential": round(ms_seq / ms_bat, 3)}
+    res = {"workload": "3M Gaussians (128 clusters, 40^3 box, seed 6), 8 x 1920x1080, L1 + 0.2(1-SSIM)",
+           "sequential_ms_per_view": round(ms_seq / len(views), 4), "batched_ms_per_view": round(ms_bat / len(views), 4),
+           "batched_over_sequential": round(ms_seq / ms_bat, 3)}
+    if cpu:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        vb = webgs.view_bytes(views[0])
+        target_cpu = oracle.forward_f32(vb, webgs.perturb_scene(packed, n, 99, 0.01, 0.02), n, threads=threads,
+                                        keys=False)["rgb"]
+        c = cpu_forward_backward(vb, packed, n, target_cpu, threads)
+        res["cpu_baseline"] = {"value": round(w * h / c["ms"] / 1e3, 4), "unit": "Mpix/s", "ms_per_view": c["ms"],
+                               "cores": threads, "kind": "port", "passes_ms": c["passes_ms"],
+                               "sample": "view 0 of the 8: fp32 frame, FP64 loss, FP64 adjoint"}
+    return res
 
 
 if __name__ == "__main__":

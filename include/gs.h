@@ -31,6 +31,8 @@ extern "C" {
 #define GS_ERR_CUDA 5      /* a CUDA runtime call failed; gs_last_error() has the message */
 #define GS_ERR_STATE 6     /* call out of order, e.g. backward without a matching forward */
 #define GS_ERR_UNSUPPORTED 7
+#define GS_ERR_MEMORY 8    /* checked builds only: a store index fell outside its buffer, or a canary
+                              pad around a device buffer was overwritten (GS_DEV_BOUNDS / _CANARY) */
 
 /* ---- memory location of caller buffers -------------------------------------------------------- */
 #define GS_MEM_HOST 0      /* pageable or pinned host memory; the call is synchronous */
@@ -55,6 +57,18 @@ typedef struct gs_view {
     float texture_size[2];/* image width, height in pixels (as floats) */
     uint32_t pad0, pad1;
 } gs_view;
+
+/* A camera as the reference's Camera class holds it (src/renderer/camera.js: eye, the point looked at,
+ * the world up vector, the vertical field of view, the canvas size, and Z_NEAR / Z_FAR): the input of
+ * Camera.getUniform() (camera.js:87-98), 56 bytes. */
+typedef struct gs_camera {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float fovy_deg;        /* vertical field of view in degrees, in (0, 180) */
+    uint32_t width, height;/* image size in pixels */
+    float z_near, z_far;   /* 0 < z_near < z_far */
+} gs_camera;
 
 /* Tunables. Defaults are the reference's constants (renderer.js:16-26). */
 typedef struct gs_config {
@@ -91,6 +105,8 @@ typedef struct gs_frame_info {
 
 #define GS_DEV_OVERFLOW 1u
 #define GS_DEV_TIMEOUT 2u
+#define GS_DEV_BOUNDS 4u   /* checked builds: a store was skipped because its index was out of bounds */
+#define GS_DEV_CANARY 8u   /* checked builds: a canary pad around a device buffer was found overwritten */
 
 /* Intermediate buffers of the last frame, copied to host for parity checks. Any pointer may be
  * NULL. Sizes: N = scene count, T = tiles_x * tiles_y, capacity = entries of keys/vals. */
@@ -161,6 +177,25 @@ typedef struct gs_batch_view {
  * location. Same results as gs_forward per view. */
 int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count);
 
+/* One view of a batch given by its camera: the 176-byte block is built on the device. */
+typedef struct gs_batch_camera {
+    const gs_scene* scene;
+    gs_camera camera;
+    gs_image out;
+} gs_batch_camera;
+
+/* gs_forward_batch with the view blocks built on the device (no counterpart in the reference, which
+ * builds one block per frame on the host, camera.js:87-98 + renderer.js:773-797): the batch uploads
+ * its 56-byte cameras, and the graph's first kernel builds every view's block from them, the same
+ * bits as gs_camera_view. Results equal gs_forward_batch with those blocks. GS_ERR_INVALID for a
+ * camera gs_camera_view would reject. */
+int gs_forward_batch_cameras(gs_ctx* ctx, const gs_batch_camera* views, uint32_t count);
+
+/* Camera.getUniform() (camera.js:87-98) for n cameras on the device (no counterpart in the
+ * reference): the same bits as gs_camera_view per camera. cams: host memory; out: n blocks in
+ * `location` (host: synchronous; device: stream-ordered). */
+int gs_camera_views(gs_ctx* ctx, const gs_camera* cams, uint32_t n, gs_view* out, int32_t location);
+
 /* Counters of the last forward (synchronizes). */
 int gs_get_frame_info(gs_ctx* ctx, gs_frame_info* info);
 /* Counters of view `index` of the last gs_forward_batch (synchronizes). */
@@ -223,8 +258,22 @@ int gs_check_wait_timeout(gs_ctx* ctx);
  * this hook a test reaches that call without running 2^26 frames. Synchronous. */
 int gs_debug_set_sequence(gs_ctx* ctx, uint32_t seq);
 
+/* 1 for libwebgs_checked.so, 0 for the product library. The checked build (the stand-in for a
+ * memory sanitizer, which is not available here) pads every device buffer of a context with canary
+ * words that a kernel verifies after each forward, batch and backward, and tests every
+ * data-dependent store index against its buffer; a violation sets GS_DEV_BOUNDS / GS_DEV_CANARY and
+ * the call returns GS_ERR_MEMORY. */
+int gs_checked_build(void);
+/* Checked builds: overwrites one canary word after the last frame's sorted-keys buffer (inside the
+ * pad the build allocated there), from the host, so a test can see the next frame report it.
+ * Product builds: GS_ERR_UNSUPPORTED. */
+int gs_debug_damage_canary(gs_ctx* ctx);
+
 /* The pinned fp32 exp of the kernels, evaluated on the device (y = exp(x)). */
 int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
+/* The raster's pinned exp (alpha = o * exp(power), raseter.wgsl:89), defined for x in [-5.6, 0], on
+ * the device: for parity tests against the oracle. */
+int gs_raster_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
 
 /* Exclusive scan for callers that must not allocate device memory (no counterpart in the
  * reference). Same result as gs_exclusive_scan, but it needs no context and calls no cudaMalloc,

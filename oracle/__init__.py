@@ -47,6 +47,7 @@ def load() -> C.CDLL:
         lib.oracle_expf.restype = C.c_float
         lib.oracle_expf.argtypes = [C.c_float]
         lib.oracle_expf_array.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+        lib.oracle_raster_expf_array.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
         lib.oracle_radix_sort_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]
         lib.oracle_exclusive_scan.restype = C.c_uint32
         lib.oracle_exclusive_scan.argtypes = [C.c_void_p, C.c_uint32]
@@ -126,6 +127,14 @@ def expf(x: np.ndarray) -> np.ndarray:
     xx = np.ascontiguousarray(x, dtype=np.float32)
     y = np.empty_like(xx)
     load().oracle_expf_array(xx.ctypes.data, y.ctypes.data, xx.size)
+    return y
+
+
+def raster_expf(x: np.ndarray) -> np.ndarray:
+    """The raster's exp (rule 4b of gs_oracle.h), defined for x in [-5.6, 0]."""
+    xx = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(xx)
+    load().oracle_raster_expf_array(xx.ctypes.data, y.ctypes.data, xx.size)
     return y
 
 

@@ -62,13 +62,48 @@ float pinned_expf(float x) {
     return (p * s1) * s2;
 }
 
+// The raster's exp (rule 4b): the alpha of raseter.wgsl:89 evaluates exp only between a splat's
+// cut-off (>= ln(1/255) - 1e-3 > -5.6) and 0, so no range checks are needed there. n = rint(x log2 e)
+// by one fma with the 1.5 * 2^23 shift (the sum's low mantissa bits are n), r = x - n ln2 by one fma
+// (|n| <= 8 here, so the f32 ln2 alone keeps r within 1.6e-8 of x - n ln2), e^r by a degree-6
+// polynomial with c0 = c1 = 1 whose c2..c6 are the project's relative-error minimax fit on
+// [-ln2/2, ln2/2] (Remez exchange; 4.3e-9 relative before rounding), and 2^n from the shift's bits.
+// Every step is an IEEE-754 operation.
+float raster_expf(float x) {
+    const float t = std::fmaf(x, 0x1.715476p+0f, 12582912.0f);
+    const float n = t - 12582912.0f;
+    const float r = std::fmaf(-n, 0x1.62e43p-1f, x);
+    float p = 0x1.6c350cp-10f;
+    p = std::fmaf(p, r, 0x1.1246dap-7f);
+    p = std::fmaf(p, r, 0x1.555638p-5f);
+    p = std::fmaf(p, r, 0x1.55547ep-3f);
+    p = std::fmaf(p, r, 0x1.fffffep-2f);
+    p = std::fmaf(p, r, 1.0f);
+    p = std::fmaf(p, r, 1.0f);
+    uint32_t tb;
+    std::memcpy(&tb, &t, 4);
+    const uint32_t sb = (tb + 127u) << 23;  // (n + 127) << 23: the shift's own exponent bits drop out
+    float scale;
+    std::memcpy(&scale, &sb, 4);
+    return p * scale;
+}
+
+// The raster's alpha exp over every argument the WGSL evaluates it at (power <= 0). The CUDA raster
+// evaluates it only from the splat's cut-off up (power >= ln((1/255)/o) - 1e-3 > -5.6 for any o in
+// [0, 1]; a pixel below skips, its alpha being below 1/255 for sure); here raster_expf covers
+// [-5.6, 0] and the general pinned exp the arguments below, where any value keeps alpha below 1/255
+// and so gives the same skip. (A NaN opacity makes alpha 0.99 whatever exp returns, in both.)
+float alpha_expf(float x) { return x >= -5.6f ? raster_expf(x) : pinned_expf(x); }
+
 template <class T> struct Num;
 template <> struct Num<float> {
     static float ex(float x) { return pinned_expf(x); }
+    static float ex_raster(float x) { return alpha_expf(x); }
     static float fma(float a, float b, float c) { return std::fmaf(a, b, c); }
 };
 template <> struct Num<double> {
     static double ex(double x) { return std::exp(x); }
+    static double ex_raster(double x) { return std::exp(x); }
     static double fma(double a, double b, double c) { return std::fma(a, b, c); }
 };
 
@@ -478,7 +513,7 @@ void raster(const Uniforms& u, uint32_t tile, const uint32_t* ranges, const uint
                     const T q = Num<T>::fma(a * dx, dx, (cc * dy) * dy);
                     const T power = Num<T>::fma((T)-0.5f, q, -((b * dx) * dy));
                     if (power > (T)0) continue;
-                    const T alpha = tmin((T)kAlphaClamp, o * Num<T>::ex(power));
+                    const T alpha = tmin((T)kAlphaClamp, o * Num<T>::ex_raster(power));
                     if (alpha < (T)kEpsilon) continue;
                     const T testT = Tr * ((T)1 - alpha);
                     if (testT < (T)kBlendThreshold) break;  // done = true; the loop ends
@@ -590,6 +625,10 @@ int forward(const void* uniforms, const float* packed, uint32_t n, uint32_t tile
 extern "C" {
 
 float oracle_expf(float x) { return pinned_expf(x); }
+
+void oracle_raster_expf_array(const float* x, float* y, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = raster_expf(x[i]);
+}
 
 void oracle_expf_array(const float* x, float* y, uint64_t n) {
     for (uint64_t i = 0; i < n; ++i) y[i] = pinned_expf(x[i]);
@@ -1005,10 +1044,13 @@ struct SsimWindow {
     }
 };
 // separable correlation with zero padding, one channel plane (H x W)
+// Rows (then columns) are independent, so the loops run on all host cores; every output element is
+// the same sum in the same order as on one core.
 void blur(const std::vector<double>& in, std::vector<double>& out, uint32_t W, uint32_t H, const SsimWindow& k) {
     std::vector<double> tmp((size_t)W * H, 0.0);
-    for (uint32_t y = 0; y < H; ++y)
-        for (uint32_t x = 0; x < W; ++x) {
+#pragma omp parallel for schedule(static)
+    for (int64_t yi = 0; yi < (int64_t)H; ++yi)
+        for (uint32_t x = 0, y = (uint32_t)yi; x < W; ++x) {
             double s = 0;
             for (int i = -5; i <= 5; ++i) {
                 const int xx = (int)x + i;
@@ -1017,8 +1059,9 @@ void blur(const std::vector<double>& in, std::vector<double>& out, uint32_t W, u
             tmp[(size_t)y * W + x] = s;
         }
     out.assign((size_t)W * H, 0.0);
-    for (uint32_t y = 0; y < H; ++y)
-        for (uint32_t x = 0; x < W; ++x) {
+#pragma omp parallel for schedule(static)
+    for (int64_t yi = 0; yi < (int64_t)H; ++yi)
+        for (uint32_t x = 0, y = (uint32_t)yi; x < W; ++x) {
             double s = 0;
             for (int i = -5; i <= 5; ++i) {
                 const int yy = (int)y + i;
@@ -1041,19 +1084,24 @@ double loss_l1_ssim(const double* X, const double* Yi, uint32_t W, uint32_t H, d
     l1 /= (double)(3 * P);
     for (int ch = 0; ch < 3; ++ch) {
         std::vector<double> x(P), y(P), xx(P), yy(P), xy(P);
-        for (size_t i = 0; i < P; ++i) {
+#pragma omp parallel for schedule(static)
+        for (int64_t ii = 0; ii < (int64_t)P; ++ii) {
+            const size_t i = (size_t)ii;
             x[i] = X[3 * i + ch]; y[i] = Yi[3 * i + ch];
             xx[i] = x[i] * x[i]; yy[i] = y[i] * y[i]; xy[i] = x[i] * y[i];
         }
         std::vector<double> mx, my, mxx, myy, mxy;
         blur(x, mx, W, H, k); blur(y, my, W, H, k); blur(xx, mxx, W, H, k); blur(yy, myy, W, H, k); blur(xy, mxy, W, H, k);
         std::vector<double> d1(P), d2(P), d3(P);  // dS/dm1, dS/dm2(=dS/dsxx), dS/dmxy(=dS/dsxy)
-        for (size_t i = 0; i < P; ++i) {
+        std::vector<double> smap(P);
+#pragma omp parallel for schedule(static)
+        for (int64_t ii = 0; ii < (int64_t)P; ++ii) {
+            const size_t i = (size_t)ii;
             const double sxx = mxx[i] - mx[i] * mx[i], syy = myy[i] - my[i] * my[i], sxy = mxy[i] - mx[i] * my[i];
             const double A1 = 2 * mx[i] * my[i] + C1, A2 = 2 * sxy + C2;
             const double B1 = mx[i] * mx[i] + my[i] * my[i] + C1, B2 = sxx + syy + C2;
             const double s = A1 * A2 / (B1 * B2);
-            ssim_sum += s;
+            smap[i] = s;
             const double ds_dmx = (2 * my[i] * A2) / (B1 * B2) - s * (2 * mx[i]) / B1;
             const double ds_dsxx = -s / B2;
             const double ds_dsxy = 2 * A1 / (B1 * B2);
@@ -1061,11 +1109,16 @@ double loss_l1_ssim(const double* X, const double* Yi, uint32_t W, uint32_t H, d
             d2[i] = ds_dsxx;
             d3[i] = ds_dsxy;
         }
+        for (size_t i = 0; i < P; ++i) ssim_sum += smap[i];  // in index order, as on one core
         if (grad) {
             std::vector<double> b1, b2, b3;
             blur(d1, b1, W, H, k); blur(d2, b2, W, H, k); blur(d3, b3, W, H, k);
             const double scale = -lambda / (double)(3 * P);
-            for (size_t i = 0; i < P; ++i) grad[3 * i + ch] += scale * (b1[i] + 2 * x[i] * b2[i] + y[i] * b3[i]);
+#pragma omp parallel for schedule(static)
+            for (int64_t ii = 0; ii < (int64_t)P; ++ii) {
+                const size_t i = (size_t)ii;
+                grad[3 * i + ch] += scale * (b1[i] + 2 * x[i] * b2[i] + y[i] * b3[i]);
+            }
         }
     }
     return l1 + lambda * (1.0 - ssim_sum / (double)(3 * P));

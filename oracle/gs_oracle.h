@@ -24,6 +24,9 @@
  *      with dot summed in component order.
  *   4. exp(x) = the pinned exp of oracle_expf() (Cody-Waite reduction by ln 2 and a degree-7
  *      Taylor polynomial in Horner form with fma), sigmoid(x) = 1 / (1 + exp(-x)).
+ *   4b. the raster's alpha (raseter.wgsl:89) uses the raster exp of oracle_raster_expf_array():
+ *      arguments in [-5.6, 0] only, one-fma reduction by ln 2 and a degree-6 minimax polynomial
+ *      (under 2 ulp from exp; WGSL allows 3 + 2|x| ulp).
  *   5. raster: power = fma(-0.5, fma(a*dx, dx, (c*dy)*dy), -((b*dx)*dy));
  *              color_k = fma(color_k_splat * alpha, T, color_k).
  *   6. mat*vec and mat*mat: each element is a dot product summed in index order.
@@ -83,6 +86,8 @@ int oracle_forward_f64(const void* uniforms, const float* packed, uint32_t n, ui
 /* The pinned fp32 exp (rule 4), exposed so tests can compare it with the CUDA kernels. */
 float oracle_expf(float x);
 void oracle_expf_array(const float* x, float* y, uint64_t n);
+/* The raster's exp (rule 4b), defined for x in [-5.6, 0]. */
+void oracle_raster_expf_array(const float* x, float* y, uint64_t n);
 
 /* Literal restatement of the reference radix sort (count / scan / reorder over 256-element blocks,
  * radix_parallel.wgsl:26-160) on arbitrary pairs, sorting on `passes` 8-bit digits from bit 0. */

@@ -17,10 +17,13 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def built_libraries():
-    """Builds libwebgs.so and the oracle library once per session (incremental)."""
+    """Builds libwebgs.so and the oracle library once per session (incremental); with WEBGS_CHECKED=1
+    also the checked build, which the tests then load instead of the product library."""
+    import os
+
     from build import build_all  # web-gs-renderer_gb300/build.py
 
-    build_all()
+    build_all(checked=os.environ.get("WEBGS_CHECKED") == "1")
     yield
 
 

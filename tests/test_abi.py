@@ -135,3 +135,9 @@ def test_perturb_scene_moves_only_means_and_sh():
     assert 0.005 < d[: 3 * n].std() < 0.015
     assert np.all(d[3 * n: 10 * n] == 0) and np.all(d[13 * n: 14 * n] == 0)
     assert 0.01 < d[10 * n: 13 * n].std() < 0.03 and 0.015 < d[14 * n:].std() < 0.025
+
+
+def test_product_library_is_not_the_checked_build():
+    lib = webgs.library()
+    assert lib.gs_checked_build() == 0
+    assert lib.gs_debug_damage_canary(None) == _abi.GS_ERR_INVALID

@@ -90,6 +90,52 @@ def test_autotune_picks_a_valid_configuration():
         assert ctx.config.sort_block == cfg["sort_block"]
 
 
+def _batch_ms(cfg: dict, items_spec, packs, reps: int = 30) -> float:
+    """Best of three timings of `reps` device-output batches (wall clock around a synchronized queue
+    of launches; the queue keeps the GPU busy, so this is the device time per batch)."""
+    import time
+
+    import torch
+
+    specs, cams = items_spec
+    with webgs.Context(**cfg) as ctx:
+        scs = [ctx.upload(p, s.count) for s, p in zip(specs, packs)]
+        imgs = [torch.empty(c.width * c.height, dtype=torch.int32, device="cuda") for _, c in cams]
+        arr = (webgs._abi.BatchView * len(cams))()
+        for k, (si, c) in enumerate(cams):
+            arr[k].scene = scs[si].handle
+            arr[k].view = c.view()
+            arr[k].out = webgs._abi.Image(webgs.GS_MEM_DEVICE, imgs[k].data_ptr(), None, None, None)
+        lib = webgs.library()
+        best = float("inf")
+        for _ in range(3):
+            for _ in range(3):
+                ctx._ck(lib.gs_forward_batch(ctx.handle, arr, len(cams)))
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                ctx._ck(lib.gs_forward_batch(ctx.handle, arr, len(cams)))
+            ctx.synchronize()
+            best = min(best, (time.perf_counter() - t0) / reps * 1e3)
+        for sc in scs:
+            sc.close()
+    return best
+
+
+def test_autotune_pick_is_not_slower_than_the_defaults():
+    """The pick re-timed on the batch it was tuned on: no slower than the default configuration (5%
+    allowance for run-to-run noise; the sweep's last stage already re-times its three best
+    candidates with four times as many batches)."""
+    specs = [W.SceneSpec(150_000, 5, 1, 64, 20.0), W.SceneSpec(400_000, 4, 1, 64, 20.0)]
+    packs = [s.build() for s in specs]
+    cams = [(i % 2, c) for i, (_, c) in enumerate(W.orbit_cameras(6, 31, 9.0))]
+    cfg, _ = webgs.autotune_scenes([(p, s.count) for s, p in zip(specs, packs)], [c.view() for _, c in cams],
+                                   [si for si, _ in cams], iters=3)
+    tuned = _batch_ms(cfg, (specs, cams), packs)
+    default = _batch_ms({}, (specs, cams), packs)
+    assert tuned <= default * 1.05, (cfg, tuned, default)
+
+
 def test_autotune_over_several_scenes():
     specs = [W.SceneSpec(8_000, 7, 0), W.SceneSpec(12_000, 8, 1, 16, 8.0)]
     scenes = [(s.build(), s.count) for s in specs]

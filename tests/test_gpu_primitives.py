@@ -70,3 +70,14 @@ def test_pinned_exp_bitwise(gpu_ctx):
     g = gpu_ctx.exp(x)
     o = oracle.expf(x)
     np.testing.assert_array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_raster_exp_bitwise(gpu_ctx):
+    """The raster's exp (its own pinned definition on [-5.6, 0]) on the device equals the oracle's."""
+    rng = np.random.default_rng(1)
+    x = np.concatenate([np.linspace(-5.6, 0.0, 1_000_001, dtype=np.float32),
+                        rng.uniform(-5.6, 0.0, 2_000_000).astype(np.float32),
+                        np.array([0.0, -0.0, -5.6, -1e-30, -1e-8, -0.3465736, -0.3465736 * 3], np.float32)])
+    g = gpu_ctx.exp(x, raster=True)
+    o = oracle.raster_expf(x)
+    np.testing.assert_array_equal(g.view(np.uint32), o.view(np.uint32))

@@ -182,6 +182,19 @@ def test_pinned_exp_accuracy():
     assert special[4] == 0.0 and np.isnan(special[5])
 
 
+def test_raster_exp_accuracy():
+    """The raster's exp (rule 4b) on its whole domain [-5.6, 0]: under 1 ulp from the FP64 exp
+    (WGSL allows 3 + 2|x| ulp for exp)."""
+    x = np.concatenate([np.linspace(-5.6, 0.0, 2_000_001, dtype=np.float32),
+                        np.random.default_rng(3).uniform(-5.6, 0.0, 500_000).astype(np.float32),
+                        np.array([0.0, -0.0, -1e-30, -1e-8], np.float32)])
+    y = oracle.raster_expf(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    ulp = np.abs(y - ref) / np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert ulp.max() < 1.0, ulp.max()
+    assert oracle.raster_expf(np.array([0.0], np.float32))[0] == 1.0
+
+
 def test_fp64_twin_close_to_fp32():
     packed = webgs.synth_scene(0, 2000, 5)
     v = camera(96, 80)

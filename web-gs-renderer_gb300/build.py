@@ -21,6 +21,9 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "libwebgs.so"
+# the checked build (-DGS_CHECKED): canary-padded buffers and bounds-checked stores, a test-only library
+BUILD_CHECKED = PKG / "_build_checked"
+LIB_CHECKED = PKG / "lib" / "libwebgs_checked.so"
 ORACLE_SRC = ROOT / "oracle" / "gs_oracle.cpp"
 ORACLE_INPUTS = ROOT / "oracle" / "gs_inputs.cpp"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
@@ -64,28 +67,31 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build_library(force: bool = False) -> Path:
-    """Compiles libwebgs.so for sm_103a (nvcc cross-compiles without a GPU)."""
-    BUILD.mkdir(exist_ok=True)
-    LIB.parent.mkdir(exist_ok=True)
+def build_library(force: bool = False, checked: bool = False) -> Path:
+    """Compiles libwebgs.so for sm_103a (nvcc cross-compiles without a GPU); with checked=True the
+    checked build libwebgs_checked.so instead."""
+    build_dir, lib = (BUILD_CHECKED, LIB_CHECKED) if checked else (BUILD, LIB)
+    extra = ["-DGS_CHECKED"] if checked else []
+    build_dir.mkdir(exist_ok=True)
+    lib.parent.mkdir(exist_ok=True)
     nvcc = _nvcc()
     headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "gs.h"]
     jobs, objs = [], []
     for src in sorted(CSRC.glob("*.cu")):
-        obj = BUILD / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers + [Path(__file__)]):
-            jobs.append([nvcc, *_nvcc_flags(src), "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *_nvcc_flags(src), *extra, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
     for src in sorted(CSRC.glob("*.cpp")):
-        obj = BUILD / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers + [Path(__file__)]):
-            jobs.append(["g++", *CXX_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
+            jobs.append(["g++", *CXX_FLAGS, *extra, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"])
+    return lib
 
 
 def build_oracle(force: bool = False) -> Path:
@@ -97,12 +103,14 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_all(force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        a = ex.submit(build_library, force)
-        b = ex.submit(build_oracle, force)
-        a.result()
-        b.result()
+def build_all(force: bool = False, checked: bool = False) -> None:
+    """The product library and the oracle; with checked=True also the checked build."""
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        jobs = [ex.submit(build_library, force), ex.submit(build_oracle, force)]
+        if checked:
+            jobs.append(ex.submit(build_library, force, True))
+        for j in jobs:
+            j.result()
 
 
 if __name__ == "__main__":

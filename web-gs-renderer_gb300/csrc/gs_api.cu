@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gs.h"
+#include "gs_camera.h"
 #include "gs_kernels.h"
 
 using namespace gs;
@@ -23,24 +24,54 @@ namespace {
 
 const char* kNoCtxError = "invalid context";
 
+// A device buffer that grows on demand. In checked builds every allocation carries a canary pad of
+// kCanaryBytes (kCanaryWord repeated) on either side, which k_check_canaries verifies after frames.
 template <class T> struct DevBuf {
     T* p = nullptr;
     size_t cap = 0;  // elements
+#ifdef GS_CHECKED
+    char* raw = nullptr;
+#endif
     cudaError_t reserve(size_t n) {
         if (n <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
+        release();
         const size_t want = std::max<size_t>(n, 1);
+#ifdef GS_CHECKED
+        const size_t bytes = want * sizeof(T);
+        cudaError_t e = cudaMalloc(&raw, bytes + 2 * kCanaryBytes);
+        if (e != cudaSuccess) { raw = nullptr; return e; }
+        e = cudaMemset(raw, 0xA5, kCanaryBytes);
+        if (e == cudaSuccess) e = cudaMemset(raw + kCanaryBytes + bytes, 0xA5, kCanaryBytes);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) { cudaFree(raw); raw = nullptr; return e; }
+        p = reinterpret_cast<T*>(raw + kCanaryBytes);
+#else
         cudaError_t e = cudaMalloc(&p, want * sizeof(T));
         if (e != cudaSuccess) { p = nullptr; return e; }
+#endif
         cap = want;
         return cudaSuccess;
     }
     void release() {
+#ifdef GS_CHECKED
+        if (raw) cudaFree(raw);
+        raw = nullptr;
+#else
         if (p) cudaFree(p);
+#endif
         p = nullptr;
         cap = 0;
+    }
+    // checked builds: appends this buffer's two pads to the list
+    void pads(CanaryList& l) const {
+#ifdef GS_CHECKED
+        if (!raw || l.count >= kCanaryListMax) return;
+        l.head[l.count] = reinterpret_cast<const uint32_t*>(raw);
+        l.tail[l.count] = reinterpret_cast<const uint32_t*>(raw + kCanaryBytes + cap * sizeof(T));
+        ++l.count;
+#else
+        (void)l;
+#endif
     }
 };
 
@@ -63,6 +94,7 @@ struct Frame {
     DevBuf<uint64_t> flags;
     DevBuf<uint32_t> ranges;
     DevBuf<uint32_t> order;  // tiles by decreasing range length: the raster CTAs' tile order
+    DevBuf<uint32_t> order_hist;  // per-slice bin counts of the tile order (64 words per 1024 tiles)
     DevBuf<uint32_t> rgba8, n_contrib;
     DevBuf<float> rgb, final_t;
     DevBuf<float> grad2d, dl_stage;
@@ -82,11 +114,17 @@ struct Frame {
         if (e == cudaSuccess) e = cudaMemsetAsync(ctl.p, 0, sizeof(FrameCtl), s);
         return e;
     }
+    void pads(CanaryList& l) const {
+        ctl.pads(l); view.pads(l); rec.pads(l); meta.pads(l); counts.pads(l); offsets.pads(l);
+        for (int b = 0; b < 2; ++b) { keys[b].pads(l); vals[b].pads(l); }
+        flags.pads(l); ranges.pads(l); order.pads(l); order_hist.pads(l); rgba8.pads(l); n_contrib.pads(l);
+        rgb.pads(l); final_t.pads(l); grad2d.pads(l); dl_stage.pads(l);
+    }
     void release() {
         ctl.release(); view.release(); rec.release(); meta.release(); counts.release(); offsets.release();
         for (int b = 0; b < 2; ++b) { keys[b].release(); vals[b].release(); }
         flags.release(); ranges.release(); rgba8.release(); n_contrib.release(); rgb.release(); final_t.release();
-        order.release(); grad2d.release(); dl_stage.release();
+        order.release(); order_hist.release(); grad2d.release(); dl_stage.release();
         if (h_ctl) cudaFreeHost(h_ctl);
         h_ctl = nullptr;
     }
@@ -147,9 +185,11 @@ struct gs_ctx {
     cudaEvent_t slot_done[kViewSlots] = {};
     uint32_t next_slot = 0;
     ViewBlock* h_bviews = nullptr;  // batch view blocks (pinned), capacity bviews_cap
+    gs_camera* h_bcams = nullptr;   // batch cameras (pinned), capacity bviews_cap
     uint32_t bviews_cap = 0;
     cudaEvent_t bviews_done = nullptr;
     DevBuf<ViewBlock> d_bviews;
+    DevBuf<gs_camera> d_bcams;
 
     // profiling
     cudaEvent_t ev[kPassCount + 1] = {};
@@ -174,7 +214,25 @@ int cuda_fail(gs_ctx* ctx, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);      \
     } while (0)
 
+// Checked builds: enqueues the canary check of a frame's buffers and the context's shared ones; a
+// damaged pad sets kDevCanary in the frame's status word. Product builds: nothing.
+void check_canaries(gs_ctx* ctx, const Frame& f, cudaStream_t s) {
+#ifdef GS_CHECKED
+    CanaryList l{};
+    f.pads(l);
+    ctx->aux_ctl.pads(l); ctx->aux_flags.pads(l); ctx->aux_u32.pads(l); ctx->aux_f32.pads(l);
+    ctx->grad_stage.pads(l); ctx->loss_scratch.pads(l); ctx->loss_io.pads(l); ctx->loss_sums.pads(l);
+    ctx->d_bviews.pads(l); ctx->d_bcams.pads(l);
+    launch_check_canaries(l, &f.ctl.p->status, s);
+#else
+    (void)ctx; (void)f; (void)s;
+#endif
+}
+
 int status_to_code(gs_ctx* ctx, uint32_t status) {
+    if (status & (kDevBounds | kDevCanary))
+        return fail(ctx, GS_ERR_MEMORY, status & kDevBounds ? "a store index fell outside its buffer (checked build)"
+                                                             : "a canary pad around a device buffer was overwritten");
     if (status & kDevTimeout) return fail(ctx, GS_ERR_TIMEOUT, "a device-side wait hit its iteration limit");
     if (status & kDevOverflow)
         return fail(ctx, GS_ERR_OVERFLOW, "instance count exceeded max_instance; output truncated");
@@ -217,7 +275,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     const uint32_t radix = 1u << ctx->cfg.digit_bits;
     const void* before[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
                             f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p,
-                            f.order.p};
+                            f.order.p, f.order_hist.p};
     GS_CK(f.rec.reserve((size_t)a.n * kRecFloat4));
     GS_CK(f.meta.reserve(a.n));
     GS_CK(f.counts.reserve(((size_t)a.n + 1 + 7) / 8 * 8));
@@ -235,6 +293,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     }
     GS_CK(f.ranges.reserve((size_t)a.tiles_x * a.tiles_y * 2));
     GS_CK(f.order.reserve((size_t)a.tiles_x * a.tiles_y));
+    GS_CK(f.order_hist.reserve((size_t)tile_order_slices(a.tiles_x * a.tiles_y) * 64));
     const size_t pix = (size_t)a.w * a.h;
     GS_CK(f.rgba8.reserve(pix));
     GS_CK(f.rgb.reserve(pix * 3));
@@ -242,7 +301,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     GS_CK(f.n_contrib.reserve(pix));
     const void* after[] = {f.rec.p, f.meta.p, f.counts.p, f.offsets.p, f.keys[0].p, f.keys[1].p, f.vals[0].p,
                            f.vals[1].p, f.flags.p, f.ranges.p, f.rgba8.p, f.rgb.p, f.final_t.p, f.n_contrib.p,
-                            f.order.p};
+                            f.order.p, f.order_hist.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) ++ctx->alloc_gen;
     return GS_OK;
 }
@@ -316,7 +375,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
     launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, a.max_instance, 0, s);
-    launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order.p, s);
+    launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order_hist.p, f.order.p, &ctl->status, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
     launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,
                   a.tiles_x, a.tiles_y, a.out, f.order.p, s);
@@ -355,13 +414,23 @@ int copy_outputs(gs_ctx* ctx, Frame& f, const gs_image* out, cudaStream_t s) {
     return GS_OK;
 }
 
+// A batch whose view blocks are built on the device: the graph's first kernel fills `views` from
+// `cams` (count cameras) before any frame reads them.
+struct CameraPrologue {
+    const gs_camera* cams = nullptr;
+    ViewBlock* views = nullptr;
+    uint32_t count = 0;
+};
+
 int capture_and_launch(gs_ctx* ctx, cudaGraphExec_t* exec, GraphKey* cached, const GraphKey& key,
-                       const std::vector<Frame*>& frames, const std::vector<FrameArgs>& args) {
+                       const std::vector<Frame*>& frames, const std::vector<FrameArgs>& args,
+                       const CameraPrologue& prologue = CameraPrologue{}) {
     if (!*exec || !(key == *cached)) {
         if (*exec) cudaGraphExecDestroy(*exec);
         *exec = nullptr;
         cudaGraph_t g = nullptr;
         GS_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        if (prologue.cams) launch_camera_views(prologue.cams, prologue.count, prologue.views, ctx->stream);
         if (frames.size() == 1) {
             enqueue_frame(ctx, *frames[0], args[0], ctx->stream, false);
         } else {
@@ -526,6 +595,7 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     if (ctx->bviews_done) cudaEventDestroy(ctx->bviews_done);
     if (ctx->h_views) cudaFreeHost(ctx->h_views);
     if (ctx->h_bviews) cudaFreeHost(ctx->h_bviews);
+    if (ctx->h_bcams) cudaFreeHost(ctx->h_bcams);
     if (ctx->h_aux) cudaFreeHost(ctx->h_aux);
     ctx->main.release();
     for (Frame* f : ctx->batch) {
@@ -534,7 +604,7 @@ int gs_ctx_destroy(gs_ctx* ctx) {
     }
     ctx->aux_ctl.release(); ctx->aux_flags.release(); ctx->aux_u32.release(); ctx->aux_f32.release();
     ctx->grad_stage.release(); ctx->loss_scratch.release(); ctx->loss_io.release();
-    ctx->loss_sums.release(); ctx->d_bviews.release();
+    ctx->loss_sums.release(); ctx->d_bviews.release(); ctx->d_bcams.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GS_OK;
@@ -661,6 +731,7 @@ int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs
     remember(f, a);
     ctx->have_timing = false;
     ctx->have_bwd = false;
+    check_canaries(ctx, f, ctx->stream);
     GS_CK(cudaMemcpyAsync(f.h_ctl, f.ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost, ctx->stream));
     rc = copy_outputs(ctx, f, out, ctx->stream);
     if (rc != GS_OK) return rc;
@@ -675,9 +746,9 @@ int gs_forward(gs_ctx* ctx, const gs_scene* scene, const gs_view* view, const gs
     return GS_OK;
 }
 
-int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
-    if (!ctx) return GS_ERR_INVALID;
-    if (!views || count == 0) return fail(ctx, GS_ERR_INVALID, "gs_forward_batch: no views");
+// gs_forward_batch and gs_forward_batch_cameras: with cams, the view blocks of `views` are ignored
+// (only their texture sizes are read on the host) and built on the device from cams.
+static int forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count, const gs_camera* cams) {
     const int32_t loc = views[0].out.location;
     for (uint32_t i = 0; i < count; ++i)
         if (views[i].out.location != loc || (loc != GS_MEM_HOST && loc != GS_MEM_DEVICE))
@@ -696,13 +767,17 @@ int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
     if (count > ctx->bviews_cap) {
         GS_CK(cudaStreamSynchronize(ctx->stream));
         if (ctx->h_bviews) cudaFreeHost(ctx->h_bviews);
+        if (ctx->h_bcams) cudaFreeHost(ctx->h_bcams);
         ctx->h_bviews = nullptr;
+        ctx->h_bcams = nullptr;
         ctx->bviews_cap = 0;
         GS_CK(cudaMallocHost(&ctx->h_bviews, sizeof(ViewBlock) * count));
+        GS_CK(cudaMallocHost(&ctx->h_bcams, sizeof(gs_camera) * count));
         ctx->bviews_cap = count;
-        const void* before = ctx->d_bviews.p;
+        const void* before[2] = {ctx->d_bviews.p, ctx->d_bcams.p};
         GS_CK(ctx->d_bviews.reserve(count));
-        if (before != ctx->d_bviews.p) ++ctx->alloc_gen;
+        GS_CK(ctx->d_bcams.reserve(count));
+        if (before[0] != ctx->d_bviews.p || before[1] != ctx->d_bcams.p) ++ctx->alloc_gen;
     }
     std::vector<FrameArgs> args(count);
     std::vector<Frame*> frames(ctx->batch.begin(), ctx->batch.begin() + count);
@@ -720,16 +795,29 @@ int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
                                      args[i].out.n_contrib});
         k.dims.insert(k.dims.end(), {args[i].n, args[i].w, args[i].h});
     }
+    k.dims.push_back(cams ? 1u : 0u);  // a graph that builds its view blocks is a different graph
     k.alloc_gen = ctx->alloc_gen;
     GS_CK(cudaEventSynchronize(ctx->bviews_done));
-    for (uint32_t i = 0; i < count; ++i) std::memcpy(&ctx->h_bviews[i], &views[i].view, sizeof(ViewBlock));
-    GS_CK(cudaMemcpyAsync(ctx->d_bviews.p, ctx->h_bviews, sizeof(ViewBlock) * count, cudaMemcpyHostToDevice, ctx->stream));
+    CameraPrologue prologue;
+    if (cams) {
+        std::memcpy(ctx->h_bcams, cams, sizeof(gs_camera) * count);
+        GS_CK(cudaMemcpyAsync(ctx->d_bcams.p, ctx->h_bcams, sizeof(gs_camera) * count, cudaMemcpyHostToDevice,
+                              ctx->stream));
+        prologue.cams = ctx->d_bcams.p;
+        prologue.views = ctx->d_bviews.p;
+        prologue.count = count;
+    } else {
+        for (uint32_t i = 0; i < count; ++i) std::memcpy(&ctx->h_bviews[i], &views[i].view, sizeof(ViewBlock));
+        GS_CK(cudaMemcpyAsync(ctx->d_bviews.p, ctx->h_bviews, sizeof(ViewBlock) * count, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    }
     GS_CK(cudaEventRecord(ctx->bviews_done, ctx->stream));
-    int rc = capture_and_launch(ctx, &ctx->exec_batch, &ctx->key_batch, k, frames, args);
+    int rc = capture_and_launch(ctx, &ctx->exec_batch, &ctx->key_batch, k, frames, args, prologue);
     if (rc != GS_OK) return rc;
     GS_CK(cudaGetLastError());
     for (uint32_t i = 0; i < count; ++i) {
         remember(*frames[i], args[i]);
+        check_canaries(ctx, *frames[i], ctx->stream);
         GS_CK(cudaMemcpyAsync(frames[i]->h_ctl, frames[i]->ctl.p, offsetof(FrameCtl, tickets), cudaMemcpyDeviceToHost,
                               ctx->stream));
         rc = copy_outputs(ctx, *frames[i], &views[i].out, ctx->stream);
@@ -742,6 +830,56 @@ int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
         for (uint32_t i = 0; i < count; ++i) status |= frames[i]->h_ctl->status;
         return status_to_code(ctx, status);
     }
+    return GS_OK;
+}
+
+int gs_forward_batch(gs_ctx* ctx, const gs_batch_view* views, uint32_t count) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!views || count == 0) return fail(ctx, GS_ERR_INVALID, "gs_forward_batch: no views");
+    return forward_batch(ctx, views, count, nullptr);
+}
+
+int gs_forward_batch_cameras(gs_ctx* ctx, const gs_batch_camera* views, uint32_t count) {
+    if (!ctx) return GS_ERR_INVALID;
+    if (!views || count == 0) return fail(ctx, GS_ERR_INVALID, "gs_forward_batch_cameras: no views");
+    std::vector<gs_batch_view> bv(count);
+    std::vector<gs_camera> cams(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        if (!gs_cam::camera_valid(views[i].camera))
+            return fail(ctx, GS_ERR_INVALID, "gs_forward_batch_cameras: view " + std::to_string(i) + ": bad camera");
+        cams[i] = views[i].camera;
+        bv[i].scene = views[i].scene;
+        bv[i].out = views[i].out;
+        std::memset(&bv[i].view, 0, sizeof(gs_view));
+        bv[i].view.texture_size[0] = (float)views[i].camera.width;
+        bv[i].view.texture_size[1] = (float)views[i].camera.height;
+    }
+    return forward_batch(ctx, bv.data(), count, cams.data());
+}
+
+int gs_camera_views(gs_ctx* ctx, const gs_camera* cams, uint32_t n, gs_view* out, int32_t location) {
+    if (!ctx) return GS_ERR_INVALID;
+    if ((!cams || !out) && n) return fail(ctx, GS_ERR_INVALID, "gs_camera_views: null buffer");
+    if (location != GS_MEM_HOST && location != GS_MEM_DEVICE) return fail(ctx, GS_ERR_INVALID, "gs_camera_views: bad location");
+    for (uint32_t i = 0; i < n; ++i)
+        if (!gs_cam::camera_valid(cams[i])) return fail(ctx, GS_ERR_INVALID, "gs_camera_views: bad camera");
+    if (n == 0) return GS_OK;
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    // staging in the aux float buffer: the cameras, then (host output) the blocks
+    const size_t cam_floats = ((size_t)n * sizeof(gs_camera) + 15) / 16 * 4;
+    const size_t view_floats = (size_t)n * sizeof(ViewBlock) / 4;
+    GS_CK(ctx->aux_f32.reserve(cam_floats + view_floats));
+    gs_camera* d_cams = reinterpret_cast<gs_camera*>(ctx->aux_f32.p);
+    ViewBlock* d_views = location == GS_MEM_DEVICE ? reinterpret_cast<ViewBlock*>(out)
+                                                   : reinterpret_cast<ViewBlock*>(ctx->aux_f32.p + cam_floats);
+    if (reinterpret_cast<uintptr_t>(d_views) % 16u != 0u)
+        return fail(ctx, GS_ERR_INVALID, "gs_camera_views: device output must be 16-byte aligned");
+    GS_CK(cudaMemcpyAsync(d_cams, cams, (size_t)n * sizeof(gs_camera), cudaMemcpyHostToDevice, ctx->stream));
+    launch_camera_views(d_cams, n, d_views, ctx->stream);
+    GS_CK(cudaGetLastError());
+    if (location == GS_MEM_DEVICE) return GS_OK;
+    GS_CK(cudaMemcpyAsync(out, d_views, (size_t)n * sizeof(ViewBlock), cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
     return GS_OK;
 }
 
@@ -912,11 +1050,13 @@ int gs_backward(gs_ctx* ctx, const gs_scene* scene, const float* dl_drgb, float*
     const int rc = enqueue_backward(ctx, f, scene, dl, out, ctx->stream, profile ? ctx->bev : nullptr);
     if (rc != GS_OK) return rc;
     ctx->have_bwd = profile;
+    check_canaries(ctx, f, ctx->stream);
     GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     if (location == GS_MEM_DEVICE) return GS_OK;
     if (nfloats) GS_CK(cudaMemcpyAsync(grad_packed, out, nfloats * 4, cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
-    return status_to_code(ctx, f.h_ctl->status & kDevTimeout);
+    // an overflow was reported by the forward
+    return status_to_code(ctx, f.h_ctl->status & (kDevTimeout | kDevBounds | kDevCanary));
 }
 
 int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl_drgb, uint32_t count,
@@ -981,6 +1121,7 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
     for (uint32_t i = 0; i < count; ++i) ctx->batch[i]->grad2d_zero = true;
     for (uint32_t i = 0; i < count; ++i) {
         Frame& f = *ctx->batch[i];
+        check_canaries(ctx, f, ctx->stream);
         GS_CK(cudaMemcpyAsync(&f.h_ctl->status, &f.ctl.p->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     }
     if (location == GS_MEM_DEVICE) return GS_OK;
@@ -988,7 +1129,7 @@ int gs_backward_batch(gs_ctx* ctx, const gs_scene* scene, const float* const* dl
     GS_CK(cudaStreamSynchronize(ctx->stream));
     uint32_t status = 0;
     for (uint32_t i = 0; i < count; ++i) status |= ctx->batch[i]->h_ctl->status;
-    return status_to_code(ctx, status & kDevTimeout);  // an overflow was reported by the forward
+    return status_to_code(ctx, status & (kDevTimeout | kDevBounds | kDevCanary));  // an overflow was reported by the forward
 }
 
 int gs_loss_l1_ssim(gs_ctx* ctx, const float* rgb, const float* target, uint32_t width, uint32_t height,
@@ -1237,13 +1378,38 @@ int gs_debug_set_sequence(gs_ctx* ctx, uint32_t seq) {
     return GS_OK;
 }
 
-int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {
+int gs_checked_build(void) {
+#ifdef GS_CHECKED
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+int gs_debug_damage_canary(gs_ctx* ctx) {
+    if (!ctx) return GS_ERR_INVALID;
+#ifdef GS_CHECKED
+    Frame& f = ctx->main;
+    if (!f.keys[0].raw) return fail(ctx, GS_ERR_STATE, "gs_debug_damage_canary: no frame rendered");
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    const uint32_t zero = 0u;
+    // the first word of the tail pad: allocated memory, outside the buffer the kernels may write
+    GS_CK(cudaMemcpy(f.keys[0].raw + kCanaryBytes + f.keys[0].cap * sizeof(uint32_t), &zero, sizeof(zero),
+                     cudaMemcpyHostToDevice));
+    return GS_OK;
+#else
+    return fail(ctx, GS_ERR_UNSUPPORTED, "gs_debug_damage_canary: product build (no canaries)");
+#endif
+}
+
+static int exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location, bool raster) {
     if (!ctx) return GS_ERR_INVALID;
     if ((!x || !y) && n) return fail(ctx, GS_ERR_INVALID, "gs_exp_f32: null buffer");
     if (n == 0) return GS_OK;
     GS_CK(cudaSetDevice(ctx->cfg.device));
     if (location == GS_MEM_DEVICE) {
-        launch_exp(x, y, n, ctx->stream);
+        launch_exp(x, y, n, ctx->stream, raster);
         GS_CK(cudaGetLastError());
         return GS_OK;
     }
@@ -1251,11 +1417,19 @@ int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t locati
     float* dx = ctx->aux_f32.p;
     float* dy = dx + n;
     GS_CK(cudaMemcpyAsync(dx, x, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
-    launch_exp(dx, dy, n, ctx->stream);
+    launch_exp(dx, dy, n, ctx->stream, raster);
     GS_CK(cudaGetLastError());
     GS_CK(cudaMemcpyAsync(y, dy, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     GS_CK(cudaStreamSynchronize(ctx->stream));
     return GS_OK;
+}
+
+int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {
+    return exp_f32(ctx, x, y, n, location, false);
+}
+
+int gs_raster_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location) {
+    return exp_f32(ctx, x, y, n, location, true);
 }
 
 }  // extern "C"

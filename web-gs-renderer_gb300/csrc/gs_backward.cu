@@ -17,6 +17,12 @@
 namespace gs {
 namespace {
 
+__device__ __forceinline__ float hw_exp2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -91,8 +97,18 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
     const float dx = a.x - p.fx, dy = a.y - p.fy;
     const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
     if (pos > p.L || power > 0.0f || power < c.y) return false;
-    const float G = raster_expf(power);
-    const float og = b.y * G;
+    // The gradient's value only needs exp to a few ulp: 2^(power log2 e) by the hardware's base-2
+    // exponential (one multiply and one MUFU op; its relative error and that of the rounded argument
+    // stay under 5e-7 on the raster's range [-5.6, 0], where no result is denormal, so flushing to
+    // zero changes nothing). The decisions must be the forward's, bit for bit: alpha >= 1/255 and the
+    // 0.99 clamp are taken on o * exp(power), so where that product lies within 1e-5 (relative) of
+    // either threshold the pinned raster exp is evaluated and decides.
+    float G = hw_exp2(power * 1.44269504f);
+    float og = b.y * G;
+    if (fabsf(og - kEpsilon) <= 1e-5f * kEpsilon || fabsf(og - kAlphaClamp) <= 1e-5f * kAlphaClamp) {
+        G = raster_expf(power);
+        og = b.y * G;
+    }
     const float alpha = fminf(kAlphaClamp, og);
     if (!(alpha >= kEpsilon)) return false;
     // from here on only gradients are formed: fused multiply-adds are fine (the decisions above

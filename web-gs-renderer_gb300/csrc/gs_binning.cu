@@ -298,8 +298,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
             else if (r >= (int32_t)w) { ++q; r -= (int32_t)w; }
             const uint32_t ty = (m.x >> 16u) + q, tx = (m.x & 0xFFFFu) + (uint32_t)r;
             const uint32_t key = ((ty * tiles_x + tx) << 16u) | (m.y >> 16u);
-            keys[excl + i] = key;
-            vals[excl + i] = base + lg;
+            if (GS_IN_BOUNDS(excl + i, max_instance, &ctl->status)) {
+                keys[excl + i] = key;
+                vals[excl + i] = base + lg;
+            }
             for (uint32_t p = depth_passes; p < passes; ++p)
                 atomicAdd(&s_hist[p * radix + ((key >> (p * digit_bits)) & mask)], 1u);
         }
@@ -607,56 +609,90 @@ __device__ __forceinline__ uint32_t order_bin(uint32_t len) {
     return 63u - min(b, 63u);
 }
 
-constexpr uint32_t kOrderPer = 8;  // tiles per thread per round (8192 tiles per round of 1024 threads)
+// Two kernels over slices of kOrderSlice tiles (one CTA each): k_tile_bins writes each slice's bin
+// counts to row `slice` of a [slices x 64] table; k_tile_place gives every bin its global base (the
+// bins before it over all slices, longest first) plus the same bin's count in earlier slices, and
+// places the slice's tiles from there.
+constexpr uint32_t kOrderThreads = 256;
+constexpr uint32_t kOrderPer = 4;                                  // tiles per thread
+constexpr uint32_t kOrderSlice = kOrderThreads * kOrderPer;        // tiles per CTA
 
-__global__ void __launch_bounds__(1024) k_tile_order(const uint32_t* __restrict__ ranges, uint32_t tiles,
-                                                     uint32_t* __restrict__ order) {
-    pdl_wait();
-    __shared__ uint32_t s_bin[64];
-    const uint32_t tid = threadIdx.x;
-    if (tid < 64u) s_bin[tid] = 0u;
-    __syncthreads();
-    const uint32_t per_round = blockDim.x * kOrderPer;
-    // the bins of one round's tiles: all of its loads are issued before any is used
-    auto bins = [&](uint32_t r0, uint32_t b[kOrderPer]) {
-        uint2 r[kOrderPer];
+// the bins of the calling thread's kOrderPer tiles of slice `slice` (64 for tiles past the end);
+// all loads are issued before any is used
+__device__ __forceinline__ void slice_bins(const uint32_t* __restrict__ ranges, uint32_t tiles, uint32_t slice,
+                                           uint32_t b[kOrderPer]) {
+    uint2 r[kOrderPer];
 #pragma unroll
-        for (uint32_t k = 0; k < kOrderPer; ++k) {
-            const uint32_t t = r0 + k * blockDim.x + tid;
-            r[k] = t < tiles ? reinterpret_cast<const uint2*>(ranges)[t] : make_uint2(0u, 0u);
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < kOrderPer; ++k) b[k] = order_bin(r[k].y > r[k].x ? r[k].y - r[k].x : 0u);
-    };
-    uint32_t b[kOrderPer];
-    for (uint32_t r0 = 0; r0 < tiles; r0 += per_round) {
-        bins(r0, b);
-#pragma unroll
-        for (uint32_t k = 0; k < kOrderPer; ++k)
-            if (r0 + k * blockDim.x + tid < tiles) atomicAdd(&s_bin[b[k]], 1u);
+    for (uint32_t k = 0; k < kOrderPer; ++k) {
+        const uint32_t t = slice * kOrderSlice + k * kOrderThreads + threadIdx.x;
+        r[k] = t < tiles ? reinterpret_cast<const uint2*>(ranges)[t] : make_uint2(0u, 0u);
     }
+#pragma unroll
+    for (uint32_t k = 0; k < kOrderPer; ++k) {
+        const uint32_t t = slice * kOrderSlice + k * kOrderThreads + threadIdx.x;
+        b[k] = t < tiles ? order_bin(r[k].y > r[k].x ? r[k].y - r[k].x : 0u) : 64u;
+    }
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_tile_bins(const uint32_t* __restrict__ ranges, uint32_t tiles,
+                                                             uint32_t* __restrict__ slice_hist) {
+    pdl_wait();
+    __shared__ uint32_t s_bin[65];
+    if (threadIdx.x < 65u) s_bin[threadIdx.x] = 0u;
     __syncthreads();
-    if (tid < 32u) {  // exclusive scan of the 64 bins, two per lane
-        const uint32_t x = s_bin[2u * tid], y = s_bin[2u * tid + 1u];
-        uint32_t incl = x + y;
+    uint32_t b[kOrderPer];
+    slice_bins(ranges, tiles, blockIdx.x, b);
+#pragma unroll
+    for (uint32_t k = 0; k < kOrderPer; ++k) atomicAdd(&s_bin[b[k]], 1u);
+    __syncthreads();
+    if (threadIdx.x < 64u) slice_hist[blockIdx.x * 64u + threadIdx.x] = s_bin[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_tile_place(const uint32_t* __restrict__ ranges, uint32_t tiles,
+                                                              const uint32_t* __restrict__ slice_hist,
+                                                              uint32_t* __restrict__ order, uint32_t* status) {
+    pdl_wait();
+    __shared__ uint32_t s_incl[64];
+    __shared__ uint32_t s_base[64];
+    const uint32_t tid = threadIdx.x, slices = gridDim.x;
+    uint32_t b[kOrderPer];
+    slice_bins(ranges, tiles, blockIdx.x, b);  // in flight while the table is summed
+    uint32_t total = 0, before = 0, incl = 0;
+    if (tid < 64u) {  // warps 0 and 1: one bin per thread
+        for (uint32_t s = 0; s < slices; ++s) {
+            const uint32_t h = slice_hist[s * 64u + tid];
+            total += h;
+            before += s < blockIdx.x ? h : 0u;
+        }
+        incl = total;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (tid >= (uint32_t)o) incl += t;
+            if ((tid & 31u) >= (uint32_t)o) incl += t;
         }
-        const uint32_t excl = incl - (x + y);
-        s_bin[2u * tid] = excl;
-        s_bin[2u * tid + 1u] = excl + x;
+        s_incl[tid] = incl;
     }
     __syncthreads();
-    for (uint32_t r0 = 0; r0 < tiles; r0 += per_round) {
-        if (r0 != 0u || tiles > per_round) bins(r0, b);  // one round: the bins are still in registers
+    if (tid < 64u) s_base[tid] = (tid >= 32u ? s_incl[31] : 0u) + incl - total + before;
+    __syncthreads();
 #pragma unroll
-        for (uint32_t k = 0; k < kOrderPer; ++k) {
-            const uint32_t t = r0 + k * blockDim.x + tid;
-            if (t < tiles) order[atomicAdd(&s_bin[b[k]], 1u)] = t;
+    for (uint32_t k = 0; k < kOrderPer; ++k) {
+        const uint32_t t = blockIdx.x * kOrderSlice + k * kOrderThreads + tid;
+        if (t < tiles) {
+            const uint32_t at = atomicAdd(&s_base[b[k]], 1u);
+            if (GS_IN_BOUNDS(at, tiles, status)) order[at] = t;
         }
     }
+}
+
+// canary check: one CTA per buffer, one word of each pad per thread
+__global__ void k_check_canaries(CanaryList list, uint32_t* status) {
+    const uint32_t b = blockIdx.x;
+    if (b >= list.count) return;
+    bool bad = false;
+    for (uint32_t w = threadIdx.x; w < kCanaryBytes / 4u; w += blockDim.x)
+        bad |= list.head[b][w] != kCanaryWord || list.tail[b][w] != kCanaryWord;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, kDevCanary);
 }
 
 // SM count of the current device (contexts of one process share a GPU model; read once, and from
@@ -757,8 +793,18 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
 #undef GS_ONESWEEP
 }
 
-void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* order, cudaStream_t s) {
-    launch_pdl(k_tile_order, dim3(1), dim3(1024), s, ranges, tiles, order);
+void launch_check_canaries(const CanaryList& list, uint32_t* status, cudaStream_t s) {
+    if (list.count) k_check_canaries<<<list.count, kCanaryBytes / 4u, 0, s>>>(list, status);
+}
+
+uint32_t tile_order_slices(uint32_t tiles) { return (tiles + kOrderSlice - 1u) / kOrderSlice; }
+
+void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order,
+                       uint32_t* status, cudaStream_t s) {
+    const uint32_t slices = std::max(1u, tile_order_slices(tiles));
+    launch_pdl(k_tile_bins, dim3(slices), dim3(kOrderThreads), s, ranges, tiles, slice_hist);
+    launch_pdl(k_tile_place, dim3(slices), dim3(kOrderThreads), s, ranges, tiles, (const uint32_t*)slice_hist, order,
+               status);
 }
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,

@@ -12,6 +12,17 @@ namespace gs {
 // Device status word bits (also in gs.h as GS_DEV_*).
 constexpr uint32_t kDevOverflow = 1u;
 constexpr uint32_t kDevTimeout = 2u;
+constexpr uint32_t kDevBounds = 4u;  // checked builds: a store index outside its buffer (the store is skipped)
+constexpr uint32_t kDevCanary = 8u;  // checked builds: a canary pad around a device buffer was overwritten
+
+// Checked builds (-DGS_CHECKED, libwebgs_checked.so) test every data-dependent store index against
+// its buffer's size, skip the store and record kDevBounds instead of writing out of bounds; product
+// builds compile the test away (their indices are bounded by construction).
+#ifdef GS_CHECKED
+#define GS_IN_BOUNDS(i, n, status) ((i) < (n) ? true : (atomicOr((status), ::gs::kDevBounds), false))
+#else
+#define GS_IN_BOUNDS(i, n, status) true
+#endif
 
 // Bounded spin: a wait on another CTA's publication gives up after this many polls (about a
 // second with the back-off below; a healthy predecessor publishes within microseconds), records
@@ -100,7 +111,8 @@ __device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
 
 // Lookback word: [63:34] sequence number of the pass that wrote it, [33:32] flag, [31:0] value.
 // Words of earlier passes carry an older sequence number and read as "not ready", so the flag
-// arrays never need clearing (they are zeroed once at allocation; sequence numbers start at 16).
+// arrays are zeroed at allocation and not per pass (sequence numbers start at 16); they are cleared
+// again only on the frame where the 30-bit tags wrap to zero (k_frame_begin).
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagInclusive = 2u;
 constexpr uint32_t kSeqMask = (1u << 30) - 1u;

@@ -11,22 +11,9 @@
 #include <vector>
 
 #include "../../include/gs.h"
+#include "gs_camera.h"
 
 namespace {
-
-// ---- camera: src/renderer/camera.js:87-98 and :135-142 ---------------------------------------
-// wgpu-matrix (3.4.2, not vendored) lookAt builds the inverse of a camera frame whose z axis points
-// from the target to the eye; perspective maps view depth [near, far] to clip depth [0, 1] (WebGPU
-// convention). Both are restated here from their published definitions; the reference stores every
-// matrix in a Float32Array, so each element is rounded to f32 once.
-struct D3 { double x, y, z; };
-D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-D3 normalize(D3 a) {
-    const double l = std::sqrt(dot(a, a));
-    return l > 0 ? D3{a.x / l, a.y / l, a.z / l} : D3{0, 0, 0};
-}
 
 // ---- deterministic normal draws ------------------------------------------------------------
 // Counter-based: every (seed, stream, index) maps to its own 64-bit hash, so generation order and
@@ -114,46 +101,23 @@ void unit_quat(uint64_t seed, uint64_t stream, uint64_t i, double q[4]) {
 
 extern "C" int gs_camera_view(const float eye[3], const float target[3], const float up[3], float fovy_deg,
                               uint32_t width, uint32_t height, float z_near, float z_far, gs_view* out) {
-    if (!eye || !target || !up || !out || width == 0 || height == 0 || !(fovy_deg > 0.0f) || !(fovy_deg < 180.0f) ||
-        !(z_near > 0.0f) || !(z_far > z_near))
-        return GS_ERR_INVALID;
-    std::memset(out, 0, sizeof(*out));
-    const D3 e{eye[0], eye[1], eye[2]}, t{target[0], target[1], target[2]}, u{up[0], up[1], up[2]};
-    const D3 zA = normalize(sub(e, t));
-    const D3 xA = normalize(cross(u, zA));
-    const D3 yA = normalize(cross(zA, xA));
-    float view[16] = {(float)xA.x, (float)yA.x, (float)zA.x, 0.0f,
-                      (float)xA.y, (float)yA.y, (float)zA.y, 0.0f,
-                      (float)xA.z, (float)yA.z, (float)zA.z, 0.0f,
-                      (float)-dot(xA, e), (float)-dot(yA, e), (float)-dot(zA, e), 1.0f};
-    const double aspect = (double)width / (double)height;
-    const double fovy = (double)fovy_deg * 3.141592653589793 / 180.0;
-    const double f = std::tan(3.141592653589793 * 0.5 - 0.5 * fovy);
-    const double rangeInv = 1.0 / ((double)z_near - (double)z_far);
-    float proj[16] = {0};
-    proj[0] = (float)(f / aspect);
-    proj[5] = (float)f;
-    proj[10] = (float)((double)z_far * rangeInv);
-    proj[11] = -1.0f;
-    proj[14] = (float)((double)z_far * (double)z_near * rangeInv);
-    // mat4.multiply(projection, view): column-major product computed in double, stored as f32.
-    for (int c = 0; c < 4; ++c)
-        for (int r = 0; r < 4; ++r) {
-            double s = 0;
-            for (int k = 0; k < 4; ++k) s += (double)proj[k * 4 + r] * (double)view[c * 4 + k];
-            out->view_proj[c * 4 + r] = (float)s;
-        }
-    std::memcpy(out->view, view, sizeof(view));
-    out->camera_pos[0] = eye[0];
-    out->camera_pos[1] = eye[1];
-    out->camera_pos[2] = eye[2];
-    const double tanFovY = std::tan(fovy / 2.0), tanFovX = tanFovY * aspect;
-    out->focal[0] = (float)((double)width / (2.0 * tanFovX));
-    out->focal[1] = (float)((double)height / (2.0 * tanFovY));
-    out->tan_fov[0] = (float)tanFovX;
-    out->tan_fov[1] = (float)tanFovY;
-    out->texture_size[0] = (float)width;
-    out->texture_size[1] = (float)height;
+    if (!eye || !target || !up || !out) return GS_ERR_INVALID;
+    gs_camera c;
+    for (int k = 0; k < 3; ++k) {
+        c.eye[k] = eye[k];
+        c.target[k] = target[k];
+        c.up[k] = up[k];
+    }
+    c.fovy_deg = fovy_deg;
+    c.width = width;
+    c.height = height;
+    c.z_near = z_near;
+    c.z_far = z_far;
+    if (!gs_cam::camera_valid(c)) return GS_ERR_INVALID;
+    float block[44];
+    gs_cam::camera_block(c, block);  // the same function the device builder runs (gs_camera.h)
+    static_assert(sizeof(block) == sizeof(gs_view), "the view block is 176 bytes");
+    std::memcpy(out, block, sizeof(gs_view));
     return GS_OK;
 }
 

@@ -96,8 +96,24 @@ void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, ui
 void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, FrameCtl* ctl, uint64_t* flags,
                            uint32_t slot, cudaStream_t s, uint32_t grid = 0);
 
-// Tiles by decreasing range length (a permutation of 0..tiles-1) for the raster launches.
-void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* order, cudaStream_t s);
+// Tiles by decreasing range length (a permutation of 0..tiles-1) for the raster launches: two
+// kernels over slices of 1024 tiles. slice_hist holds 64 words per slice (tile_order_slices), fully
+// rewritten by every call.
+uint32_t tile_order_slices(uint32_t tiles);
+void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order,
+                       uint32_t* status, cudaStream_t s);
+
+// Checked builds: verifies the canary pads of up to kCanaryListMax buffers (head and tail pad of
+// kCanaryBytes each, filled with kCanaryWord) and sets kDevCanary in *status if any word changed.
+constexpr uint32_t kCanaryBytes = 256;
+constexpr uint32_t kCanaryWord = 0xA5A5A5A5u;
+constexpr uint32_t kCanaryListMax = 64;
+struct CanaryList {
+    const uint32_t* head[kCanaryListMax];
+    const uint32_t* tail[kCanaryListMax];
+    uint32_t count;
+};
+void launch_check_canaries(const CanaryList& list, uint32_t* status, cudaStream_t s);
 
 void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
                         int grid_cap, cudaStream_t s);
@@ -114,7 +130,15 @@ void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const 
                    uint32_t n, const FrameCtl* ctl, uint32_t width, uint32_t height, uint32_t tiles_x,
                    uint32_t tiles_y, const RasterOut& out, const uint32_t* order, cudaStream_t s);
 
-void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s);
+// y = the pinned exp of x (raster: the raster's exp, defined on [-5.6, 0]).
+void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s, bool raster = false);
+
+}  // namespace gs
+struct gs_camera;
+namespace gs {
+// Camera.getUniform() for n cameras on the device (gs_camera.cu): out[i] gets camera i's 176-byte
+// block, the same bits as gs_camera_view. out must be 16-byte aligned.
+void launch_camera_views(const gs_camera* cams, uint32_t n, ViewBlock* out, cudaStream_t s);
 
 // Sets the sequence number of gs_exclusive_scan_static's scratch on the current device (a test hook).
 cudaError_t static_scan_set_sequence(uint32_t seq);

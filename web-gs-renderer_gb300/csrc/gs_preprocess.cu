@@ -7,6 +7,7 @@
 // arithmetic follows the WGSL source order with no contraction (the file is built with -fmad=false)
 // so that every output bit equals the reference restatement.
 #include "gs_kernels.h"
+#include "gs_raster_common.cuh"
 
 namespace gs {
 namespace {
@@ -375,9 +376,10 @@ __global__ void __launch_bounds__(256) k_pack_to_rows(const float* __restrict__ 
     }
 }
 
+template <bool RASTER>
 __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = pinned_expf(x[i]);
+    if (i < n) y[i] = RASTER ? raster_expf(x[i]) : pinned_expf(x[i]);
 }
 
 }  // namespace
@@ -400,9 +402,10 @@ void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float
     k_pack_to_rows<<<grid, 256, 0, s>>>(packed, n, stride, rows);
 }
 
-void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s) {
+void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s, bool raster) {
     if (n == 0) return;
-    k_exp<<<(n + 255u) / 256u, 256, 0, s>>>(x, y, n);
+    if (raster) k_exp<true><<<(n + 255u) / 256u, 256, 0, s>>>(x, y, n);
+    else k_exp<false><<<(n + 255u) / 256u, 256, 0, s>>>(x, y, n);
 }
 
 }  // namespace gs

@@ -17,25 +17,26 @@
 
 namespace gs {
 
-// The pinned exp restricted to the arguments the raster can reach. For an opacity o in (0, 1] the
-// cut-off is at least ln(1/255) - 1e-3 > -5.6, so every argument lies in [-5.6, 0]: no range
-// checks are needed and 2^n (n >= -9) is applied as one exact power-of-two factor, which gives the
-// same bits as pinned_expf's two-factor scaling. o = 0 (cut-off +inf) never gets here; for a NaN
-// opacity the product o * exp(.) is NaN whatever this returns, as with pinned_expf.
-// n = rint(x * log2 e) comes from the 1.5 * 2^23 shift: for |x log2 e| < 2^22 the sum rounds to an
-// integer, to nearest even, exactly as rintf does, and its bits also give 2^n (no float-to-int
-// conversion); the result is bit-identical to the rintf form.
+// The raster's exp (alpha = o * exp(power), raseter.wgsl:89), pinned like the oracle's raster_expf.
+// For an opacity o in (0, 1] the cut-off is at least ln(1/255) - 1e-3 > -5.6, so every argument lies in
+// [-5.6, 0] and no range checks are needed. n = rint(x log2 e) comes from one fma with the 1.5 * 2^23
+// shift (the sum rounds to an integer, to nearest even, and its low mantissa bits are n, which also
+// give 2^n without a float-to-int conversion); r = x - n ln2 is one fma with the f32 ln2 (|n| <= 8, so
+// r stays within 1.6e-8 of the exact reduction); e^r is a degree-6 polynomial with c0 = c1 = 1 and
+// c2..c6 from the project's relative-error minimax fit on [-ln2/2, ln2/2]. Under 0.9 ulp from exp on
+// the range (the tests check it against the FP64 exp and bit for bit against the oracle). 11
+// instructions, against 15 for the degree-7 Taylor form of the general pinned exp.
+// o = 0 (cut-off +inf) never gets here; for a NaN opacity the product o * exp(.) is NaN whatever this
+// returns, as with pinned_expf.
 __device__ __forceinline__ float raster_expf(float x) {
-    const float t = __fadd_rn(__fmul_rn(x, 0x1.715476p+0f), 12582912.0f);
+    const float t = __fmaf_rn(x, 0x1.715476p+0f, 12582912.0f);
     const float n = __fadd_rn(t, -12582912.0f);
-    float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
-    r = __fmaf_rn(-n, -0x1.05c61p-29f, r);
-    float p = 0x1.a01a02p-13f;
-    p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
-    p = __fmaf_rn(p, r, 0x1.111112p-7f);
-    p = __fmaf_rn(p, r, 0x1.555556p-5f);
-    p = __fmaf_rn(p, r, 0x1.555556p-3f);
-    p = __fmaf_rn(p, r, 0.5f);
+    const float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
+    float p = 0x1.6c350cp-10f;
+    p = __fmaf_rn(p, r, 0x1.1246dap-7f);
+    p = __fmaf_rn(p, r, 0x1.555638p-5f);
+    p = __fmaf_rn(p, r, 0x1.55547ep-3f);
+    p = __fmaf_rn(p, r, 0x1.fffffep-2f);
     p = __fmaf_rn(p, r, 1.0f);
     p = __fmaf_rn(p, r, 1.0f);
     return __fmul_rn(p, __int_as_float((__float_as_int(t) + 127) << 23));

@@ -19,7 +19,7 @@ from ._abi import (GS_FLAG_DIFFERENTIABLE, GS_FLAG_NO_GRAPH, GS_FLAG_PROFILE, GS
                    Config, Debug, FrameInfo, Image, Timing, View)
 
 __all__ = [
-    "GsError", "Context", "Scene", "Renderer", "Camera", "View", "Config", "camera_view", "synth_scene",
+    "GsError", "Context", "Scene", "Renderer", "Camera", "View", "Config", "camera_view", "make_camera", "synth_scene",
     "perturb_scene", "view_bytes", "FLOATS_PER_GAUSSIAN", "GS_FLAG_PROFILE", "GS_FLAG_NO_GRAPH",
     "GS_FLAG_DIFFERENTIABLE", "GS_MEM_HOST", "GS_MEM_DEVICE", "library",
 ]
@@ -63,6 +63,18 @@ def camera_view(eye, target, up=(0.0, 1.0, 0.0), fovy_deg: float = 60.0, width: 
                                   int(width), int(height), float(z_near), float(z_far), C.byref(v))
     _check(rc, None, "gs_camera_view")
     return v
+
+
+def make_camera(eye, target, up=(0.0, 1.0, 0.0), fovy_deg: float = 60.0, width: int = 512, height: int = 512,
+                z_near: float = 0.2, z_far: float = 1000.0) -> "_abi.Camera":
+    """A gs_camera: what camera_view takes, for the device-side builders (camera_views,
+    forward_batch_cameras)."""
+    c = _abi.Camera()
+    c.eye[:] = [float(v) for v in eye]
+    c.target[:] = [float(v) for v in target]
+    c.up[:] = [float(v) for v in up]
+    c.fovy_deg, c.width, c.height, c.z_near, c.z_far = float(fovy_deg), int(width), int(height), float(z_near), float(z_far)
+    return c
 
 
 def view_bytes(v: View) -> bytes:
@@ -288,6 +300,32 @@ class Context:
         self._ck(library().gs_forward_batch(self.handle, arr, len(items)))
         return outs
 
+    def forward_batch_cameras(self, items: list, rgba8: bool = True, rgb: bool = False) -> list[dict]:
+        """Renders [(scene, camera), ...] in one batched launch whose view blocks are built on the
+        device from the cameras (make_camera)."""
+        arr = (_abi.BatchCamera * len(items))()
+        outs = []
+        for i, (scene, cam) in enumerate(items):
+            w, h = int(cam.width), int(cam.height)
+            res = {}
+            if rgba8:
+                res["rgba8"] = np.empty((h, w, 4), dtype=np.uint8)
+            if rgb:
+                res["rgb"] = np.empty((h, w, 3), dtype=np.float32)
+            arr[i].scene = scene.handle
+            arr[i].camera = cam
+            arr[i].out = Image(GS_MEM_HOST, _ptr(res.get("rgba8")), _ptr(res.get("rgb")), None, None)
+            outs.append(res)
+        self._ck(library().gs_forward_batch_cameras(self.handle, arr, len(items)))
+        return outs
+
+    def camera_views(self, cams: list) -> list[View]:
+        """View blocks of the cameras, built on the device (gs_camera_views)."""
+        arr = (_abi.Camera * len(cams))(*cams)
+        out = (View * len(cams))()
+        self._ck(library().gs_camera_views(self.handle, arr, len(cams), C.cast(out, C.c_void_p), GS_MEM_HOST))
+        return list(out)
+
     def batch_frame_info(self, index: int) -> dict:
         fi = FrameInfo()
         self._ck(library().gs_get_batch_frame_info(self.handle, index, C.byref(fi)))
@@ -328,10 +366,12 @@ class Context:
         """Test hook: sets the lookback sequence number of every frame control block of the context."""
         self._ck(library().gs_debug_set_sequence(self.handle, seq & 0xFFFFFFFF))
 
-    def exp(self, x: np.ndarray) -> np.ndarray:
+    def exp(self, x: np.ndarray, raster: bool = False) -> np.ndarray:
+        """The kernels' pinned exp on the device (raster=True: the raster's exp, x in [-5.6, 0])."""
         xx = np.ascontiguousarray(x, dtype=np.float32)
         y = np.empty_like(xx)
-        self._ck(library().gs_exp_f32(self.handle, _ptr(xx), _ptr(y), xx.size, GS_MEM_HOST))
+        fn = library().gs_raster_exp_f32 if raster else library().gs_exp_f32
+        self._ck(fn(self.handle, _ptr(xx), _ptr(y), xx.size, GS_MEM_HOST))
         return y
 
 

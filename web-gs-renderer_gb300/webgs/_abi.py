@@ -7,6 +7,9 @@ from pathlib import Path
 
 PKG_DIR = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG_DIR / "lib" / "libwebgs.so"
+# WEBGS_CHECKED=1 selects the checked build (canary-padded buffers, bounds-checked stores): a
+# test-only library, the stand-in for a memory sanitizer
+CHECKED_LIB_PATH = PKG_DIR / "lib" / "libwebgs_checked.so"
 HEADER_PATH = PKG_DIR.parent / "include" / "gs.h"
 
 GS_OK = 0
@@ -17,9 +20,10 @@ GS_ERR_TIMEOUT = 4
 GS_ERR_CUDA = 5
 GS_ERR_STATE = 6
 GS_ERR_UNSUPPORTED = 7
+GS_ERR_MEMORY = 8
 STATUS_NAMES = {
     0: "GS_OK", 1: "GS_ERR_INVALID", 2: "GS_ERR_OOM", 3: "GS_ERR_OVERFLOW", 4: "GS_ERR_TIMEOUT",
-    5: "GS_ERR_CUDA", 6: "GS_ERR_STATE", 7: "GS_ERR_UNSUPPORTED",
+    5: "GS_ERR_CUDA", 6: "GS_ERR_STATE", 7: "GS_ERR_UNSUPPORTED", 8: "GS_ERR_MEMORY",
 }
 
 GS_MEM_HOST = 0
@@ -29,6 +33,8 @@ GS_FLAG_NO_GRAPH = 2
 GS_FLAG_DIFFERENTIABLE = 4
 GS_DEV_OVERFLOW = 1
 GS_DEV_TIMEOUT = 2
+GS_DEV_BOUNDS = 4
+GS_DEV_CANARY = 8
 
 
 class View(C.Structure):
@@ -82,6 +88,21 @@ class BatchView(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("view", View), ("out", Image)]
 
 
+class Camera(C.Structure):
+    """gs_camera: the input of Camera.getUniform() (camera.js:87-98), 56 bytes."""
+    _fields_ = [
+        ("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("fovy_deg", C.c_float),
+        ("width", C.c_uint32), ("height", C.c_uint32), ("z_near", C.c_float), ("z_far", C.c_float),
+    ]
+
+
+assert C.sizeof(Camera) == 56
+
+
+class BatchCamera(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("out", Image)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/gs.h
 SIGNATURES = [
     ("gs_version", C.c_char_p, []),
@@ -98,6 +119,8 @@ SIGNATURES = [
     ("gs_forward", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(View), C.POINTER(Image)]),
     ("gs_get_frame_info", C.c_int, [C.c_void_p, C.POINTER(FrameInfo)]),
     ("gs_forward_batch", C.c_int, [C.c_void_p, C.POINTER(BatchView), C.c_uint32]),
+    ("gs_forward_batch_cameras", C.c_int, [C.c_void_p, C.POINTER(BatchCamera), C.c_uint32]),
+    ("gs_camera_views", C.c_int, [C.c_void_p, C.POINTER(Camera), C.c_uint32, C.c_void_p, C.c_int32]),
     ("gs_get_batch_frame_info", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(FrameInfo)]),
     ("gs_backward_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_void_p,
                                     C.c_int32]),
@@ -113,9 +136,12 @@ SIGNATURES = [
     ("gs_sort_pairs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
     ("gs_exclusive_scan", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]),
     ("gs_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
+    ("gs_raster_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
     ("gs_check_wait_timeout", C.c_int, [C.c_void_p]),
     ("gs_exclusive_scan_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("gs_debug_set_sequence", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("gs_checked_build", C.c_int, []),
+    ("gs_debug_damage_canary", C.c_int, [C.c_void_p]),
     ("gs_camera_view", C.c_int, [C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
                                  C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.POINTER(View)]),
     ("gs_synth_scene", C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_float, C.c_void_p]),
@@ -132,7 +158,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     global _LIB
     if _LIB is not None and path is None:
         return _LIB
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else (CHECKED_LIB_PATH if os.environ.get("WEBGS_CHECKED") == "1" else LIB_PATH)
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build it with web-gs-renderer_gb300/build.py (no CPU fallback exists)")
     lib = C.CDLL(str(p))

@@ -10,7 +10,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import View, camera_view, synth_scene
+from . import View, camera_view, make_camera, synth_scene
 
 
 @dataclass(frozen=True)
@@ -37,6 +37,11 @@ class CameraSpec:
 
     def view(self) -> View:
         return camera_view(self.eye, self.target, (0.0, 1.0, 0.0), self.fovy, self.width, self.height,
+                           self.z_near, self.z_far)
+
+    def camera(self):
+        """The same camera as a gs_camera, for the device-side uniform builder."""
+        return make_camera(self.eye, self.target, (0.0, 1.0, 0.0), self.fovy, self.width, self.height,
                            self.z_near, self.z_far)
 
 
