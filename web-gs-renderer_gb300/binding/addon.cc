@@ -284,6 +284,72 @@ napi_value render_batch(napi_env env, napi_callback_info info) {
     return nullptr;
 }
 
+// renderBatchCameras([{name, camera: {eye: [3], target: [3], up: [3], fovy, width, height, near, far},
+// image: Uint8Array(W*H*4)}, ...]) -- a batch whose 176-byte blocks are built on the device from the
+// cameras (the reference's Camera state, camera.js)
+napi_value render_batch_cameras(napi_env env, napi_callback_info info) {
+    size_t argc = 1;
+    napi_value argv[1];
+    Native* n = unwrap(env, info, &argc, argv);
+    uint32_t count = 0;
+    napi_get_array_length(env, argv[0], &count);
+    std::vector<gs_batch_camera> views(count);
+    auto number = [&](napi_value obj, const char* key) {
+        napi_value v;
+        double d = 0.0;
+        napi_get_named_property(env, obj, key, &v);
+        napi_get_value_double(env, v, &d);
+        return d;
+    };
+    auto vec3 = [&](napi_value obj, const char* key, float out[3]) {
+        napi_value arr, e;
+        napi_get_named_property(env, obj, key, &arr);
+        for (uint32_t k = 0; k < 3; ++k) {
+            double d = 0.0;
+            napi_get_element(env, arr, k, &e);
+            napi_get_value_double(env, e, &d);
+            out[k] = (float)d;
+        }
+    };
+    for (uint32_t i = 0; i < count; ++i) {
+        napi_value item, vname, vcam, vimage;
+        napi_get_element(env, argv[0], i, &item);
+        napi_get_named_property(env, item, "name", &vname);
+        napi_get_named_property(env, item, "camera", &vcam);
+        napi_get_named_property(env, item, "image", &vimage);
+        char name[256];
+        size_t len = 0;
+        napi_get_value_string_utf8(env, vname, name, sizeof(name), &len);
+        auto it = n->scenes.find(name);
+        if (it == n->scenes.end()) {
+            napi_throw_error(env, nullptr, (std::string("Invalid Gs buffer for name \"") + name + "\"").c_str());
+            return nullptr;
+        }
+        gs_camera& c = views[i].camera;
+        vec3(vcam, "eye", c.eye);
+        vec3(vcam, "target", c.target);
+        vec3(vcam, "up", c.up);
+        c.fovy_deg = (float)number(vcam, "fovy");
+        c.width = (uint32_t)number(vcam, "width");
+        c.height = (uint32_t)number(vcam, "height");
+        c.z_near = (float)number(vcam, "near");
+        c.z_far = (float)number(vcam, "far");
+        napi_typedarray_type type;
+        size_t length = 0;
+        void* pixels = nullptr;
+        napi_get_typedarray_info(env, vimage, &type, &length, &pixels, nullptr, nullptr);
+        if (type != napi_uint8_array || length != (size_t)c.width * c.height * 4) {
+            napi_throw_type_error(env, nullptr, "image must be a Uint8Array of W*H*4 bytes");
+            return nullptr;
+        }
+        views[i].scene = it->second;
+        views[i].out = gs_image{GS_MEM_HOST, static_cast<uint8_t*>(pixels), nullptr, nullptr, nullptr};
+    }
+    const int rc = gs_forward_batch_cameras(n->ctx, views.data(), count);
+    if (rc != GS_OK && rc != GS_ERR_OVERFLOW) return throw_status(env, rc, n->ctx);
+    return nullptr;
+}
+
 // timings() -> {label: {ms}} like profiler.js:113-121
 napi_value timings(napi_env env, napi_callback_info info) {
     size_t argc = 0;
@@ -313,6 +379,7 @@ napi_value init(napi_env env, napi_value exports) {
         {"backward", nullptr, backward, nullptr, nullptr, nullptr, napi_default, nullptr},
         {"loss", nullptr, loss, nullptr, nullptr, nullptr, napi_default, nullptr},
         {"renderBatch", nullptr, render_batch, nullptr, nullptr, nullptr, napi_default, nullptr},
+        {"renderBatchCameras", nullptr, render_batch_cameras, nullptr, nullptr, nullptr, napi_default, nullptr},
     };
     napi_value cls;
     napi_define_class(env, "Native", NAPI_AUTO_LENGTH, construct, nullptr, sizeof(methods) / sizeof(methods[0]),
