@@ -133,12 +133,15 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu --set full capture of
 # the forward frame of this workload on a GB300) and what bounds each kernel there.
-NCU_TRAFFIC_BYTES = {"preprocess": 286.5e6, "raster": 56.6e6}
-# issue-slot utilisation of the kernels bound by instruction issue (ncu smsp__issue_active, the same
-# capture): for them this, not the HBM fraction, is the efficiency measure
-NCU_ISSUE_ACTIVE = {"raster": 0.936}
+NCU_TRAFFIC_BYTES = {"preprocess": 286.5e6, "raster": 56.4e6}
+# issue-slot utilisation of the kernels bound by instruction issue (ncu smsp__issue_active, one
+# capture of the kernel at this workload): for them this, not the HBM fraction, is the efficiency measure
+NCU_ISSUE_ACTIVE = {"raster": 0.938}
+# warp instructions per launch (ncu smsp__inst_executed.sum, the same capture): the numerator of the
+# issue-rate roofline of those kernels (four issue slots per SM per cycle)
+NCU_WARP_INSTRUCTIONS = {"raster": 291.79e6}
 LIMITER = {
-    "raster": "instruction issue (ncu: issue slots busy 93.6% at full residency, DRAM 3% of peak; the "
+    "raster": "instruction issue (ncu: issue slots busy 93.8% at full residency, DRAM 3% of peak; the "
               "48-byte records are re-read from L2, so DRAM traffic is below the algorithmic bytes)",
     "preprocess": "HBM and the pinned arithmetic (ncu: 69% of DRAM peak, 70% of issue slots)",
 }
@@ -430,6 +433,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get(top), "peak_source": peak_kind,
             "algorithmic_bytes": int(bytes_per[top]), "limiter": LIMITER.get(top),
             "issue_active_ncu": NCU_ISSUE_ACTIVE.get(top)}
+    # the dominant kernel's own bound: warp instructions per launch over its event time, against four
+    # issue slots per SM per cycle at the median SM clock sampled under load
+    roof_issue = None
+    if top in NCU_WARP_INSTRUCTIONS and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+        achieved_i = NCU_WARP_INSTRUCTIONS[top] / (kernel_passes[top] * 1e-3) / 1e9
+        peak_i = sms * 4 * clocks["sm_mhz"] * 1e6 / 1e9
+        roof_issue = {"bound": "instruction issue", "kernel": top, "achieved": round(achieved_i, 1),
+                      "peak": round(peak_i, 1), "unit": "G warp-instructions/s", "frac": round(achieved_i / peak_i, 4),
+                      "warp_instructions": NCU_WARP_INSTRUCTIONS[top], "sms": sms, "sm_mhz": clocks["sm_mhz"]}
     per_pass = {k: {"ms": round(v, 4), "bytes": int(bytes_per.get(k, 0)),
                     "GBps": round(bytes_per.get(k, 0) / (v * 1e-3) / 1e9, 1) if v > 0 and k in bytes_per else None}
                 for k, v in pass_ms.items()}
@@ -443,8 +456,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                          f"{r['ms_per_frame']:.0f} ms/frame",
                "value_1core": round(r1["value"], 4), "ms_per_frame_1core": round(r1["ms_per_frame"], 1)}
 
-    # frame_begin, preprocess, scan+emit, passes x onesweep, tile ranges, tile order, raster
-    launches_per_frame = 6 + passes
+    # frame_begin, preprocess, scan+emit, passes x onesweep, tile ranges, tile bins, tile place, raster
+    launches_per_frame = 7 + passes
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -453,7 +466,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                    "instances": fi["instance_count"], "visible": fi["visible"], "sort_passes": passes},
         "e2e": {"value": round(e2e, 3), "unit": "Mpix/s", "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
                 "h2d_bytes_per_step": 176, "d2h_bytes_per_step": pixels * 4},
-        "roofline": roof, "passes": per_pass, "cpu_baseline": cpu, "clocks": clocks,
+        "roofline": roof, "roofline_issue": roof_issue, "passes": per_pass, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": launches_per_frame * args.steps,
         "fwd_bwd": {"1M_1080p": fb_1080, "500k_720p": fb_720},
         "batched_fwd_16_views": batched, "batched_fwd_bwd_8_views": batched_fb,
@@ -800,9 +813,31 @@ def batched_fwd_bwd(steps, warmup, local_rank, cpu: bool = False) -> dict:
     ms_bat = _timed(stream, batched, steps, warmup)
     sc.close()
     ctx.close()
+    # per-pass times of the eight sequential steps (a profiling context, events between the passes): the
+    # rasters and raster backwards, issue-bound and per view, are what a batch cannot share or overlap
+    pctx = webgs.Context(device=local_rank, flags=webgs.GS_FLAG_DIFFERENTIABLE | webgs.GS_FLAG_PROFILE)
+    psc = pctx.upload(packed, n)
+    acc: dict[str, float] = {}
+    for rep in range(2):
+        for k, v in enumerate(views):
+            img = _abi.Image(webgs.GS_MEM_DEVICE, None, rgbs[k].data_ptr(), None, None)
+            pctx._ck(lib.gs_forward(pctx.handle, psc.handle, C.byref(v), C.byref(img)))
+            pctx._ck(lib.gs_loss_l1_ssim(pctx.handle, rgbs[k].data_ptr(), targets[k].data_ptr(), w, h, 0.2, None,
+                                         dls[k].data_ptr(), webgs.GS_MEM_DEVICE))
+            pctx._ck(lib.gs_backward(pctx.handle, psc.handle, dls[k].data_ptr(), grads.data_ptr(),
+                                     webgs.GS_MEM_DEVICE))
+            if rep == 1:
+                for name, t in pctx.timings().items():
+                    acc[name] = acc.get(name, 0.0) + t["ms"]
+    psc.close()
+    pctx.close()
+    unshared = acc.get("raster", 0.0) + acc.get("raster backward", 0.0)
     res = {"workload": "3M Gaussians (128 clusters, 40^3 box, seed 6), 8 x 1920x1080, L1 + 0.2(1-SSIM)",
            "sequential_ms_per_view": round(ms_seq / len(views), 4), "batched_ms_per_view": round(ms_bat / len(views), 4),
-           "batched_over_sequential": round(ms_seq / ms_bat, 3)}
+           "batched_over_sequential": round(ms_seq / ms_bat, 3),
+           "passes_ms_sum_8_views": {k: round(v, 4) for k, v in acc.items()},
+           "raster_and_raster_backward_ms_8_views": round(unshared, 4),
+           "overlap_bound_batched_over_sequential": round(ms_seq / unshared, 3) if unshared > 0 else None}
     if cpu:
         import oracle
 
