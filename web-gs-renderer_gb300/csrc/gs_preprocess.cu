@@ -315,7 +315,8 @@ __global__ void __launch_bounds__(kPreGroup) k_preprocess_multi(const float* __r
     if (lt == 0) mbar_init(&s_bar, 1);
     __syncthreads();
     if (lt == 0) {
-        // g0 < n <= stride; stride and g0 are multiples of 64: 256-byte aligned slices
+        // g0 < stride (g0 < n <= stride, or g0 = 0 for an empty scene, whose stride is 64); stride and g0
+        // are multiples of 64: 256-byte aligned slices
         const uint32_t cols = min(kPreGroup, stride - g0);
         mbar_expect_tx(&s_bar, kRows * cols * 4u);
         for (int r = 0; r < kRows; ++r) bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar);
@@ -393,8 +394,10 @@ void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const Vie
 
 void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uint32_t tile, const MultiViewFrames& mv,
                              cudaStream_t s) {
-    if (n == 0 || mv.count == 0) return;
-    k_preprocess_multi<<<(n + kPreGroup - 1u) / kPreGroup, kPreGroup, 0, s>>>(rows, stride, n, tile, mv);
+    if (mv.count == 0) return;
+    // at least one CTA: with an empty scene it still writes each view's scan entry counts[n] = 0
+    const uint32_t blocks = n ? (n + kPreGroup - 1u) / kPreGroup : 1u;
+    k_preprocess_multi<<<blocks, kPreGroup, 0, s>>>(rows, stride, n, tile, mv);
 }
 
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
