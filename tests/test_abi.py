@@ -141,3 +141,12 @@ def test_product_library_is_not_the_checked_build():
     lib = webgs.library()
     assert lib.gs_checked_build() == 0
     assert lib.gs_debug_damage_canary(None) == _abi.GS_ERR_INVALID
+
+
+def test_new_entry_points_reject_null_context():
+    lib = webgs.library()
+    assert lib.gs_camera_views(None, None, 0, None, webgs.GS_MEM_HOST) == _abi.GS_ERR_INVALID
+    assert lib.gs_forward_batch_cameras(None, None, 1) == _abi.GS_ERR_INVALID
+    assert lib.gs_raster_exp_f32(None, None, None, 0, webgs.GS_MEM_HOST) == _abi.GS_ERR_INVALID
+    assert lib.gs_debug_set_sequence is not None  # a test hook (needs a GPU to do anything)
+    assert C.sizeof(_abi.Camera) == 56 and C.sizeof(_abi.BatchCamera) == C.sizeof(_abi.BatchView) - 176 + 56
