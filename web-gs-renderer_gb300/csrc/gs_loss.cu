@@ -159,10 +159,16 @@ __global__ void __launch_bounds__(kThreads) k_ssim_fwd(const float* __restrict__
 }
 
 // dL/dx from the blurred partials (same tiling and register blocking as k_ssim_fwd).
+__device__ void reduce_sums(double* __restrict__ sums, size_t blocks);
+
+// sums (may be null): block 0 also reduces the forward's per-block sums into sums[0..1], while the
+// other blocks filter, so the loss value needs no kernel of its own when a gradient is formed.
 __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__ partial, const float* __restrict__ x,
                                                        const float* __restrict__ y, uint32_t W, uint32_t H,
-                                                       Window win, float lambda, float* __restrict__ dl) {
+                                                       Window win, float lambda, float* __restrict__ dl,
+                                                       double* __restrict__ sums, size_t sum_blocks) {
     pdl_wait();
+    if (sums && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) reduce_sums(sums, sum_blocks);
     __shared__ float sp[3][kH * kPitchIn];
     __shared__ float hp[3][kH * kPitchH];
     const int ch = blockIdx.z;
@@ -245,9 +251,9 @@ __global__ void __launch_bounds__(kThreads) k_ssim_bwd(const float* __restrict__
     }
 }
 
-// sums[0..1] = column sums of the per-block partials that follow them
-__global__ void k_reduce_sums(double* __restrict__ sums, size_t blocks) {
-    pdl_wait();
+// sums[0..1] = column sums of the per-block partials that follow them, by one CTA in a fixed order
+// (the same sum on every call)
+__device__ void reduce_sums(double* __restrict__ sums, size_t blocks) {
     __shared__ double red[2][32];
     double a = 0.0, b = 0.0;
     const double* part = sums + 2;
@@ -275,6 +281,11 @@ __global__ void k_reduce_sums(double* __restrict__ sums, size_t blocks) {
             sums[1] = b;
         }
     }
+}
+
+__global__ void k_reduce_sums(double* __restrict__ sums, size_t blocks) {
+    pdl_wait();
+    reduce_sums(sums, blocks);
 }
 
 Window make_window() {
@@ -305,9 +316,10 @@ void launch_loss_l1_ssim(const float* x, const float* y, uint32_t width, uint32_
                          float* scratch, double* sums, float* dl, cudaStream_t s) {
     const Window win = make_window();
     const dim3 grid = loss_grid(width, height), block(kThreads);
+    const size_t blocks = (size_t)grid.x * grid.y * grid.z;
     launch_pdl(k_ssim_fwd, grid, block, s, x, y, width, height, win, scratch, sums + 2);
-    launch_pdl(k_reduce_sums, dim3(1), dim3(1024), s, sums, (size_t)grid.x * grid.y * grid.z);
-    if (dl) launch_pdl(k_ssim_bwd, grid, block, s, scratch, x, y, width, height, win, lambda, dl);
+    if (dl) launch_pdl(k_ssim_bwd, grid, block, s, scratch, x, y, width, height, win, lambda, dl, sums, blocks);
+    else launch_pdl(k_reduce_sums, dim3(1), dim3(1024), s, sums, blocks);
 }
 
 }  // namespace gs
