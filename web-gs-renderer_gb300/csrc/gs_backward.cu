@@ -92,11 +92,21 @@ __device__ __forceinline__ void pix_load(PixState& p, uint32_t x, uint32_t y, ui
 // division (the approximate reciprocal, 2 ulp, of 1 - alpha >= 0.01 is accurate enough for a
 // gradient). With C = sum_i alpha_i T_i c_i and T_{i+1} = T_i (1 - alpha_i),
 // dC/dalpha_i = T_i c_i - S_i / (1 - alpha_i), S_i being the colour added behind splat i.
+// FIRST: g is written rather than added to (zeros when the pixel does not contribute), so the hit's
+// accumulators need no zeroing before the lane's first pixel.
+template <bool FIRST>
 __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4& a, const float4& b,
                                          const float2& c, float g[9]) {
+    auto none = [&]() {
+        if (FIRST)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) g[k] = 0.0f;
+        return false;
+    };
+    auto acc = [&](int k, float x, float y) { g[k] = FIRST ? x * y : __fmaf_rn(x, y, g[k]); };
     const float dx = a.x - p.fx, dy = a.y - p.fy;
     const float power = __fmaf_rn(-0.5f, __fmaf_rn(a.z * dx, dx, (b.x * dy) * dy), -((a.w * dx) * dy));
-    if (pos > p.L || power > 0.0f || power < c.y) return false;
+    if (pos > p.L || power > 0.0f || power < c.y) return none();
     // The gradient's value only needs exp to a few ulp: 2^(power log2 e) by the hardware's base-2
     // exponential (one multiply and one MUFU op; its relative error and that of the rounded argument
     // stay under 5e-7 on the raster's range [-5.6, 0], where no result is denormal, so flushing to
@@ -110,15 +120,15 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
         og = b.y * G;
     }
     const float alpha = fminf(kAlphaClamp, og);
-    if (!(alpha >= kEpsilon)) return false;
+    if (!(alpha >= kEpsilon)) return none();
     // from here on only gradients are formed: fused multiply-adds are fine (the decisions above
     // follow the forward's pinned arithmetic)
     const float ria = __fdividef(1.0f, 1.0f - alpha);
     const float Tb = p.T * ria;  // transmittance in front of this splat
     const float w = alpha * Tb;
-    g[6] = __fmaf_rn(w, p.dr, g[6]);
-    g[7] = __fmaf_rn(w, p.dg, g[7]);
-    g[8] = __fmaf_rn(w, p.db, g[8]);
+    acc(6, w, p.dr);
+    acc(7, w, p.dg);
+    acc(8, w, p.db);
     const float ur = __fmaf_rn(Tb, b.z, -(p.s_r * ria));
     const float ug = __fmaf_rn(Tb, b.w, -(p.s_g * ria));
     const float ub = __fmaf_rn(Tb, c.x, -(p.s_b * ria));
@@ -130,12 +140,12 @@ __device__ __forceinline__ bool pix_step(PixState& p, uint32_t pos, const float4
         const float da = og <= kAlphaClamp ? dalpha : 0.0f;
         const float gp = da * og;  // dL/dpower
         const float gpdx = gp * dx, gpdy = gp * dy;
-        g[0] = __fmaf_rn(gp, __fmaf_rn(a.z, dx, a.w * dy), g[0]);
-        g[1] = __fmaf_rn(gp, __fmaf_rn(b.x, dy, a.w * dx), g[1]);
-        g[2] = __fmaf_rn(gpdx, dx, g[2]);
-        g[3] = __fmaf_rn(gpdx, dy, g[3]);
-        g[4] = __fmaf_rn(gpdy, dy, g[4]);
-        g[5] = __fmaf_rn(da, G, g[5]);
+        acc(0, gp, __fmaf_rn(a.z, dx, a.w * dy));
+        acc(1, gp, __fmaf_rn(b.x, dy, a.w * dx));
+        acc(2, gpdx, dx);
+        acc(3, gpdx, dy);
+        acc(4, gpdy, dy);
+        acc(5, da, G);
     }
     p.s_r = __fmaf_rn(w, b.z, p.s_r);
     p.s_g = __fmaf_rn(w, b.w, p.s_g);
@@ -239,9 +249,9 @@ __global__ void __launch_bounds__(TILE * TILE / 2) k_raster_backward(const uint3
                     const float4 a = s_a[j];
                     const float4 b = s_b[j];
                     const float2 c = s_c[j];
-                    float g[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-                    const bool c0 = pix_step(p0, pos, a, b, c, g);
-                    const bool c1 = pix_step(p1, pos, a, b, c, g);
+                    float g[9];
+                    const bool c0 = pix_step<true>(p0, pos, a, b, c, g);
+                    const bool c1 = pix_step<false>(p1, pos, a, b, c, g);
                     if (__any_sync(0xffffffffu, c0 || c1)) {
                         const float mine = sign * warp_reduce_scatter8(g);  // total of value (lane >> 2) & 7
                         const float blue = warp_sum(g[8]);
