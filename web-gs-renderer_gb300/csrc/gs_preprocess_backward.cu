@@ -239,11 +239,11 @@ __device__ __forceinline__ void write_packed(const float (*tile)[kBwdPitch], flo
 }
 
 // One thread per Gaussian, six CTAs per SM (80 registers: the few spills cost less than the lost
-// residency). Everything a CTA reads comes in by bulk copies into shared memory, in two steps so that
-// only one memory round trip precedes any arithmetic: first the view block, the slice's tilesTouched
-// counts and 2D gradients and its 14 geometry attribute rows (one mbarrier); then, if any Gaussian of
-// the slice is visible, its 45 f_rest rows (a second mbarrier), whose arrival overlaps the geometric
-// part of the chain rule. The gradients replace the staged attributes in shared memory and the CTA
+// residency). Everything a CTA reads comes in by bulk copies into shared memory, all issued at once
+// on two mbarriers: the view block, the slice's tilesTouched counts and 2D gradients and its 14
+// geometry attribute rows on the first; its 45 f_rest rows on the second, whose arrival overlaps the
+// geometric part of the chain rule (a slice with no visible Gaussian only waits for them and writes
+// zeros). The gradients replace the staged attributes in shared memory and the CTA
 // writes its slice of the packed layout (pos | log-scale | rot | f_dc | opacity | f_rest blocks, the
 // layout gs_scene_upload takes) with coalesced stores; invisible Gaussians get zeros.
 // Reads past the slice: counts are read in whole 16-byte units (the buffer holds roundup(N + 1, 8)
@@ -290,19 +290,20 @@ __global__ void __launch_bounds__(kBwdGroup, 6) k_preprocess_backward(const floa
         bulk_g2s(s_d2, grad2d + (size_t)9 * g0, d2_bytes, &s_bar[0]);
         for (int r = 0; r < kRowRest; ++r)
             bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[0]);
+        // the f_rest rows too, at once: with the Gaussians in scene order almost every slice holds a
+        // visible one, and waiting for the counts before asking for them costs a round trip per CTA
+        mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
+        for (int r = kRowRest; r < kRows; ++r)
+            bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
     }
     wait_bar(&s_bar[0]);
     const bool vis = lt < cnt && s_cnt[lt] != 0u;
     const int any = __syncthreads_or(vis);
+    if (!any) wait_bar(&s_bar[1]);  // no bulk copy may still write into shared memory when the CTA leaves
     if (any) {
         // the slice's 2D gradients are in shared memory now (every thread passed the copy's barrier):
         // clear them in global memory for the next raster backward, which only accumulates
         for (uint32_t i = lt; i < 9u * cnt; i += kBwdGroup) grad2d[(size_t)9 * g0 + i] = 0.0f;
-        if (lt == 0) {
-            mbar_expect_tx(&s_bar[1], (kRows - kRowRest) * cols * 4u);
-            for (int r = kRowRest; r < kRows; ++r)
-                bulk_g2s(&s_rows[r][0], rows + (size_t)r * stride + g0, cols * 4u, &s_bar[1]);
-        }
         if (vis) {
             auto R_ = [&](int row) { return s_rows[row][lt]; };
             auto W_ = [&](int row, float v) { s_rows[row][lt] = v; };
