@@ -286,7 +286,7 @@ int ensure_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a) {
     }
     const size_t sort_parts = ((size_t)a.max_instance + ctx->cfg.sort_block - 1) / ctx->cfg.sort_block;
     const size_t scan_parts = ((size_t)a.n + 1 + kScanPartition - 1) / kScanPartition;
-    const size_t words = std::max(sort_parts * radix, scan_parts);
+    const size_t words = std::max(onesweep_flag_words(sort_parts, radix), scan_parts);
     if (words > f.flags.cap || !f.flags.p) {
         GS_CK(f.flags.reserve(words));
         GS_CK(cudaMemsetAsync(f.flags.p, 0, f.flags.cap * sizeof(uint64_t), ctx->stream));
@@ -370,7 +370,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
         const uint32_t split = p * bits >= 16u && w / 2u >= 2u ? w / 2u : 0u;
         launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
                         0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
-                        ctx->cfg.sort_block, split);
+                        ctx->cfg.sort_block, split, p > 0);  // the emit right before the first pass writes its inputs
         cur ^= 1;
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
@@ -1284,7 +1284,7 @@ int gs_sort_pairs(gs_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint3
     uint32_t* v0 = k0 + n;
     uint32_t* k1 = v0 + n;
     uint32_t* v1 = k1 + n;
-    const size_t words = ((size_t)n + ctx->cfg.sort_block - 1) / ctx->cfg.sort_block * radix;
+    const size_t words = onesweep_flag_words(((size_t)n + ctx->cfg.sort_block - 1) / ctx->cfg.sort_block, radix);
     if (words > ctx->aux_flags.cap || !ctx->aux_flags.p) {
         GS_CK(ctx->aux_flags.reserve(words));
         GS_CK(cudaMemsetAsync(ctx->aux_flags.p, 0, ctx->aux_flags.cap * 8, ctx->stream));

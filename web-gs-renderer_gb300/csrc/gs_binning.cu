@@ -4,7 +4,7 @@
 //   emit         src/shaders/emit.wgsl:28-66          -> k_scan_emit (fused, load-balanced)
 //   indirect arg src/shaders/indirect_arg.wgsl:14-27  -> FrameCtl counts read on the device
 //   radix sort   src/shaders/radix_parallel.wgsl      -> k_onesweep (one kernel per digit pass,
-//                                                        decoupled lookback per digit)
+//                                                        per-digit prefixes from an aggregate tree)
 //   tile ranges  src/shaders/tile_ranges.wgsl:7-34    -> k_tile_ranges
 //   range clear  renderer.js:919                      -> k_frame_begin(_multi) (with the counters reset)
 //
@@ -137,7 +137,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
                                                             uint32_t* __restrict__ offsets, uint32_t* __restrict__ keys,
                                                             uint32_t* __restrict__ vals, FrameCtl* ctl,
                                                             uint64_t* flags, uint32_t slot) {
-    pdl_wait();
     __shared__ uint32_t s_off[kScanPartition + 1];
     __shared__ uint2 s_meta[kScanPartition];  // (minX | minY << 16, rect width | depth16 << 16)
     __shared__ uint32_t s_own[kScanPartition];  // owner (local Gaussian) of each slot of an emit chunk
@@ -145,6 +144,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
     __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
     __shared__ uint32_t s_part, s_excl, s_seq;
 
+    // the ticket counter and the sequence number were set by the frame's first kernel, two launches
+    // back: the partition is taken before the wait for the preprocess, whose counts are read after it
     const uint32_t tid = threadIdx.x;
     if (tid == 0) {
         s_part = atomicAdd(&ctl->tickets[slot], 1u);
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_emit(const uint32_t* __re
     }
     const uint32_t radix = 1u << digit_bits;
     for (uint32_t i = tid; i < passes * radix; i += kScanThreads) s_hist[i] = 0u;
+    pdl_wait();
     __syncthreads();
     const uint32_t part = s_part, seq = s_seq;
     const uint32_t entries = n + 1u;
@@ -373,6 +375,34 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
         if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
 }
 
+// Sum of the values of `count` (1..7) tagged words p[0], p[-stride], ..., p[-(count-1) stride]: every
+// load is issued before the first is waited on; a word without this pass's tag is polled (bounded:
+// on expiry the timeout is recorded and the word counts as zero).
+__device__ __forceinline__ uint32_t sum_tagged(const uint64_t* p, size_t stride, uint32_t count, uint32_t want,
+                                               uint32_t* status) {
+    uint64_t w[7];
+#pragma unroll
+    for (uint32_t q = 0; q < 7u; ++q) w[q] = q < count ? ld_relaxed_u64(p - q * stride) : 0ull;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < 7u; ++q) {
+        if (q >= count) break;
+        uint64_t v = w[q];
+        uint32_t spins = 0;
+        while (word_seq(v) != want || word_flag(v) == 0u) {
+            if (++spins > kSpinLimit) {
+                atomicOr(status, kDevTimeout);
+                v = make_word(want, kFlagAggregate, 0u);
+                break;
+            }
+            if (spins > 64u) __nanosleep(64);
+            v = ld_relaxed_u64(p - q * stride);
+        }
+        sum += word_value(v);
+    }
+    return sum;
+}
+
 // ---- onesweep radix pass ------------------------------------------------------------------------
 // One stable counting-sort pass on digit (key >> shift) & (RADIX-1) (radix_parallel.wgsl:26-160 in
 // one kernel). Persistent CTAs take partitions of 256 x ITEMS keys (4096 or 2048) by ticket. Per
@@ -387,9 +417,15 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 //     warp, and their two passes take 16 us less per frame with SPLIT = w/2 of a w-bit digit, while
 //     the depth passes, whose warps hold few distinct digits, are fastest with the plain match);
 //   - ranks (< 4096) are kept two per register, which keeps the thread within 64 registers;
-//   - per-digit warp counts are scanned across warps (warp order = index order), the CTA's digit
-//     totals are published as lookback aggregates and the inclusive prefix of every digit is found
-//     by decoupled lookback (one thread per digit);
+//   - per-digit warp counts are scanned across warps (warp order = index order) and the CTA's digit
+//     totals are published; every digit's count in the earlier partitions comes from a tree of
+//     aggregates built inside the pass (one thread per digit): level 0 holds the partitions' totals,
+//     level L+1 the sums of groups of 8 level-L nodes, each published by the partition that completes
+//     the group; partition p sums the earlier siblings of its node at every level (the base-8 digits
+//     of p: at most 7 words per level, loaded together). All partitions of a pass publish their
+//     totals at about the same time, so the prefixes are ready a few memory round trips later at
+//     every partition, where a decoupled lookback passes inclusive prefixes along the partitions a
+//     few per round trip (on the 1M / 1080p frame the last of 536 partitions waited about 7 us);
 //   - keys/values are staged in shared memory in local sorted order and written out at
 //     global_digit_base + rank, which keeps runs of equal digits contiguous in global memory.
 template <int BITS, int ITEMS, int SPLIT>
@@ -398,8 +434,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                            const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
                                                            uint32_t dmask, const uint32_t* __restrict__ hist,
-                                                           FrameCtl* ctl, uint64_t* flags, uint32_t slot) {
-    pdl_wait();
+                                                           FrameCtl* ctl, uint64_t* flags, uint32_t slot,
+                                                           uint32_t early) {
+    // early: n, the histogram and the ticket counter were written before the previous kernel, so
+    // each CTA takes its first partition and computes the digit bases before waiting for that
+    // kernel (only the keys and values it wrote are read after the wait)
+    if (!early) pdl_wait();
     constexpr uint32_t RADIX = 1u << BITS;
     const uint32_t MASK = dmask & (RADIX - 1u);  // digit mask of this pass (narrower on a last partial digit)
     constexpr uint32_t WARPS = kSortThreads / 32;
@@ -418,7 +458,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     const uint32_t nparts = (n + PART - 1u) / PART;
 
     if (tid == 0) s_seq = ctl->seq + slot;
-    bool have_bases = false;
+    bool have_bases = false, waited = early == 0u;
 
     while (true) {
         __syncthreads();
@@ -433,6 +473,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             const uint32_t ex = block_exclusive_scan<kSortThreads>(h, s_warp, &tot);
             if (tid < RADIX) s_gbase[tid] = ex;
             have_bases = true;
+        }
+        if (!waited) {
+            pdl_wait();
+            waited = true;
         }
         const uint32_t base = part * PART;
         const uint32_t valid_n = min(PART, n - base);
@@ -474,7 +518,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
         }
         __syncthreads();
 
-        // per digit: exclusive over warps, CTA total, lookback
+        // per digit: exclusive over warps, CTA total (published at once, level 0 of the tree)
         uint32_t cta_total = 0;
         if (tid < RADIX) {
 #pragma unroll
@@ -483,8 +527,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                 s_whist[w][tid] = cta_total;
                 cta_total += c;
             }
-            st_relaxed_u64(flags + (size_t)part * RADIX + tid,
-                           make_word(seq, part == 0 ? kFlagInclusive : kFlagAggregate, cta_total));
+            st_relaxed_u64(flags + (size_t)part * RADIX + tid, make_word(seq, kFlagAggregate, cta_total));
         }
         uint32_t dtot;
         const uint32_t dstart = block_exclusive_scan<kSortThreads>(tid < RADIX ? cta_total : 0u, s_warp, &dtot);
@@ -492,41 +535,27 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             // each warp's slot base of this digit: the digit's local sorted start plus the warps before
 #pragma unroll
             for (uint32_t w = 0; w < WARPS; ++w) s_whist[w][tid] += dstart;
-            // lookback per digit (one thread per digit, bounded waits): the words of the next
-            // kLookWidth predecessors are loaded together, so a walk over partitions that have only
-            // published aggregates costs one memory round trip per kLookWidth steps
-            uint32_t excl = 0;
-            if (part != 0) {
-                constexpr int kLookWidth = 4;
-                int64_t j = (int64_t)part - 1;
-                const uint32_t want = seq & kSeqMask;
-                bool found = false;
-                while (!found && j >= 0) {
-                    uint64_t w[kLookWidth];
-#pragma unroll
-                    for (int q = 0; q < kLookWidth; ++q)
-                        w[q] = j - q >= 0 ? ld_relaxed_u64(flags + (size_t)(j - q) * RADIX + tid) : 0ull;
-#pragma unroll
-                    for (int q = 0; q < kLookWidth; ++q) {
-                        if (found || j - q < 0) break;
-                        const uint64_t* p = flags + (size_t)(j - q) * RADIX + tid;
-                        uint64_t v = w[q];
-                        uint32_t spins = 0;
-                        while (word_seq(v) != want || word_flag(v) == 0u) {
-                            if (++spins > kSpinLimit) {
-                                atomicOr(&ctl->status, kDevTimeout);
-                                v = make_word(want, kFlagInclusive, 0u);
-                                break;
-                            }
-                            if (spins > 64u) __nanosleep(64);
-                            v = ld_relaxed_u64(p);
-                        }
-                        excl += word_value(v);
-                        found = word_flag(v) == kFlagInclusive;
-                    }
-                    j -= kLookWidth;
+            // the digit's count in all earlier partitions, from the aggregate tree (one thread per
+            // digit, bounded waits): at level L the earlier siblings of the partition's own node are
+            // summed (the base-8 digit L of its index, at most 7 words, loaded together), and the
+            // partition whose node completes a group of 8 publishes the group's sum one level up
+            const uint32_t want = seq & kSeqMask;
+            uint32_t excl = 0, node = cta_total, idx = part, rows = nparts;
+            size_t base = 0;
+            bool completes = true;  // this partition is the last one of its node at the current level
+            while (idx) {
+                const uint32_t a = idx & 7u;
+                const uint32_t sib =
+                    a ? sum_tagged(flags + base + (size_t)(idx - 1u) * RADIX + tid, RADIX, a, want, &ctl->status) : 0u;
+                excl += sib;
+                completes = completes && a == 7u;
+                base += (size_t)rows * RADIX;
+                rows = (rows + 7u) >> 3;
+                idx >>= 3;
+                if (completes) {
+                    node += sib;
+                    st_relaxed_u64(flags + base + (size_t)idx * RADIX + tid, make_word(seq, kFlagAggregate, node));
                 }
-                st_relaxed_u64(flags + (size_t)part * RADIX + tid, make_word(seq, kFlagInclusive, excl + cta_total));
             }
             s_out[tid] = s_gbase[tid] + excl - dstart;
         }
@@ -767,7 +796,7 @@ void configure_sort_kernels() {
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s, uint32_t block, uint32_t split) {
+                     int grid_cap, cudaStream_t s, uint32_t block, uint32_t split, bool early) {
     const bool small = block == kSortPartitionMin;
     const uint32_t part = small ? kSortPartitionMin : kSortPartition;
     uint32_t parts = (max_n + part - 1u) / part;
@@ -776,7 +805,7 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
     if (parts == 0) parts = 1;
 #define GS_ONESWEEP(B, I, S)                                                                                      \
     launch_pdl(k_onesweep<B, I, S>, dim3(parts), dim3(kSortThreads), s, keys_in, vals_in, keys_out, vals_out, n_dev, \
-               n_host, shift, dmask, hist, ctl, flags, slot)
+               n_host, shift, dmask, hist, ctl, flags, slot, early ? 1u : 0u)
 #define GS_ONESWEEP_SPLIT(I)                             \
     switch (split) {                                     \
         case 2: GS_ONESWEEP(8, I, 2); break;             \

@@ -77,7 +77,17 @@ void launch_scan_emit(const uint32_t* counts, const uint4* meta, uint32_t n, uin
                       uint32_t digit_bits, uint32_t passes, uint32_t* offsets, uint32_t* keys, uint32_t* vals,
                       FrameCtl* ctl, uint64_t* flags, uint32_t slot, cudaStream_t s);
 
-// Onesweep LSD radix pass. n comes from *n_dev when non-null, else n_host.
+// Onesweep LSD radix pass. n comes from *n_dev when non-null, else n_host. flags must hold
+// onesweep_flag_words(partitions, radix) words for the largest partition count the pass can see (the
+// partitions' digit totals and the aggregate tree above them, 8 nodes per parent).
+inline size_t onesweep_flag_words(size_t parts, uint32_t radix) {
+    size_t words = 0;
+    for (size_t rows = parts;; rows = (rows + 7) / 8) {
+        words += rows * radix;
+        if (rows <= 1) break;
+    }
+    return words;
+}
 constexpr uint32_t kSortThreads = 256;
 constexpr uint32_t kSortItems = 16;                            // keys per thread of the largest block
 constexpr uint32_t kSortPartition = kSortThreads * kSortItems; // largest sort block (4096 keys)
@@ -87,7 +97,10 @@ void configure_sort_kernels();
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s, uint32_t block = kSortPartition, uint32_t split = 0);
+                     int grid_cap, cudaStream_t s, uint32_t block = kSortPartition, uint32_t split = 0,
+                     bool early = false);
+// early: *n_dev (or n_host), hist, ctl->seq and the ticket counter were written at least two kernels
+// back on the stream, so they are read before the programmatic-launch wait for the previous kernel.
 // Digit histograms of all passes over the low key_bits bits, for a standalone sort.
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);
