@@ -535,10 +535,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             // each warp's slot base of this digit: the digit's local sorted start plus the warps before
 #pragma unroll
             for (uint32_t w = 0; w < WARPS; ++w) s_whist[w][tid] += dstart;
-            // the digit's count in all earlier partitions, from the aggregate tree (one thread per
-            // digit, bounded waits): at level L the earlier siblings of the partition's own node are
-            // summed (the base-8 digit L of its index, at most 7 words, loaded together), and the
-            // partition whose node completes a group of 8 publishes the group's sum one level up
+        }
+        // the digit's count in all earlier partitions, from the aggregate tree (one thread per digit,
+        // bounded waits): at level L the earlier siblings of the partition's own node are summed (the
+        // base-8 digit L of its index, at most 7 words, loaded together), and the partition whose node
+        // completes a group of 8 publishes the group's sum one level up
+        auto prefix = [&]() {
             const uint32_t want = seq & kSeqMask;
             uint32_t excl = 0, node = cta_total, idx = part, rows = nparts;
             size_t base = 0;
@@ -558,7 +560,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                 }
             }
             s_out[tid] = s_gbase[tid] + excl - dstart;
-        }
+        };
+        // a partition that completes a group of 8 builds its tree nodes at once; the others first put
+        // their keys in local sorted order, which needs no global prefix, and read the tree after
+        // that, when more of it is complete
+        const bool builds = (part & 7u) == 7u;
+        if (builds && tid < RADIX) prefix();
         __syncthreads();
 
         // local sorted order in shared memory; values are read only now, straight into their slot,
@@ -573,6 +580,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                 s_vals[pos] = vals_in[idx];
             }
         }
+        if (!builds && tid < RADIX) prefix();
         __syncthreads();
         for (uint32_t i = tid; i < valid_n; i += kSortThreads) {
             const uint32_t k = s_keys[i];
