@@ -123,9 +123,10 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
         "preprocess": 12 * n + 224 * npass + 4 * n + 48 * npass + 16 * vis,
         # counts + rects in, offsets + keys/values out
         "scan+emit": 4 * (n + 1) + 16 * vis + 4 * (n + 1) + 8 * s,
-        # each pass reads and writes keys and values
+        # each pass reads and writes keys and values (the last one also leaves the tile ranges)
         "sort": passes * 16 * s,
-        "tile ranges": 4 * s + 8 * tiles,
+        # the ranges read twice (bin counts, placement), the order written
+        "tile order": 2 * 8 * tiles + 4 * tiles,
         # per instance the index and the 48 B record, per tile its range, per pixel 4 B rgba8
         "raster": 52 * s + 8 * tiles + 4 * pixels,
     }
@@ -456,8 +457,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                          f"{r['ms_per_frame']:.0f} ms/frame",
                "value_1core": round(r1["value"], 4), "ms_per_frame_1core": round(r1["ms_per_frame"], 1)}
 
-    # frame_begin, preprocess, scan+emit, passes x onesweep, tile ranges, tile bins, tile place, raster
-    launches_per_frame = 7 + passes
+    # frame_begin, preprocess, scan+emit, passes x onesweep, tile bins, tile place, raster
+    launches_per_frame = 6 + passes
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",

@@ -80,7 +80,7 @@ uint32_t bitlen(uint32_t v) { return v == 0 ? 0u : 32u - (uint32_t)__builtin_clz
 constexpr int kViewSlots = 16;
 constexpr int kSideStreams = 16;
 enum Pass { kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
-const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile ranges", "raster"};
+const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile order", "raster"};
 
 // Everything one view's frame needs on the device, and what the last frame on it was.
 struct Frame {
@@ -370,11 +370,11 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
         const uint32_t split = p * bits >= 16u && w / 2u >= 2u ? w / 2u : 0u;
         launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
                         0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
-                        ctx->cfg.sort_block, split, p > 0);  // the emit right before the first pass writes its inputs
+                        ctx->cfg.sort_block, split, p > 0,  // the emit right before the first pass writes its inputs
+                        p + 1 == a.passes ? f.ranges.p : nullptr, a.tiles_x * a.tiles_y);  // the last pass: ranges
         cur ^= 1;
     }
     if (profile) cudaEventRecord(ctx->ev[3], s);
-    launch_tile_ranges(f.keys[cur].p, ctl, a.tiles_x * a.tiles_y, f.ranges.p, a.max_instance, 0, s);
     launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order_hist.p, f.order.p, &ctl->status, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
     launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,

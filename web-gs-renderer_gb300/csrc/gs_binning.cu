@@ -5,7 +5,8 @@
 //   indirect arg src/shaders/indirect_arg.wgsl:14-27  -> FrameCtl counts read on the device
 //   radix sort   src/shaders/radix_parallel.wgsl      -> k_onesweep (one kernel per digit pass,
 //                                                        per-digit prefixes from an aggregate tree)
-//   tile ranges  src/shaders/tile_ranges.wgsl:7-34    -> k_tile_ranges
+//   tile ranges  src/shaders/tile_ranges.wgsl:7-34    -> the last k_onesweep pass (run bounds by
+//                                                        min / max) + k_tile_place (empty tiles)
 //   range clear  renderer.js:919                      -> k_frame_begin(_multi) (with the counters reset)
 //
 // Ordering: every kernel that chains partitions takes a ticket from FrameCtl so that partition p
@@ -75,7 +76,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
 }
 
 // Resets one frame's control block (CTA 0) and clears its tile ranges (renderer.js:919) with
-// 16-byte stores across the CTAs [0, ncta), the tail word by word.
+// 16-byte stores across the CTAs [0, ncta), the tail word by word. A range is cleared to
+// (0xFFFFFFFF, 0), the identities of the min / max the last sort pass combines the tile's bounds with;
+// the tile order kernel writes (0, 0), the reference's cleared value, back into the tiles left empty.
 //
 // Lookback words carry only the low 30 bits of the sequence number, which advances by 16 per frame,
 // so the tags repeat every 2^26 frames: a word left from 2^26 frames earlier with a set flag would
@@ -85,11 +88,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
 __device__ __forceinline__ void frame_begin(FrameCtl* ctl, uint32_t* ranges, uint32_t range_words, uint64_t* flags,
                                             uint32_t flag_words, uint32_t cta, uint32_t ncta) {
     const uint32_t t = threadIdx.x;
-    const uint32_t quads = range_words / 4u;
+    const uint32_t quads = range_words / 4u;  // range_words is even: (start, end) pairs
     for (uint32_t q = cta * blockDim.x + t; q < quads; q += ncta * blockDim.x)
-        reinterpret_cast<uint4*>(ranges)[q] = make_uint4(0u, 0u, 0u, 0u);
+        reinterpret_cast<uint4*>(ranges)[q] = make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
     if (cta != 0) return;
-    for (uint32_t i = quads * 4u + t; i < range_words; i += blockDim.x) ranges[i] = 0u;
+    for (uint32_t i = quads * 4u + t; i < range_words; i += blockDim.x) ranges[i] = (i & 1u) ? 0u : 0xFFFFFFFFu;
     const uint32_t next = (ctl->seq & ~15u) + 16u;
     __syncthreads();  // every thread has read the old sequence number before thread 0 replaces it
     if (t == 0) {
@@ -435,7 +438,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                                                            const uint32_t* n_dev, uint32_t n_host, uint32_t shift,
                                                            uint32_t dmask, const uint32_t* __restrict__ hist,
                                                            FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                                                           uint32_t early) {
+                                                           uint32_t early, uint32_t* __restrict__ ranges,
+                                                           uint32_t tiles) {
     // early: n, the histogram and the ticket counter were written before the previous kernel, so
     // each CTA takes its first partition and computes the digit bases before waiting for that
     // kernel (only the keys and values it wrote are read after the wait)
@@ -588,46 +592,17 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             if (gpos < n) {  // always true unless a lookback timed out (status already set)
                 keys_out[gpos] = k;
                 vals_out[gpos] = s_vals[i];
-            }
-        }
-    }
-}
-
-// ---- tile ranges (tile_ranges.wgsl:7-34) over the sorted prefix -----------------------------------
-// Each thread takes four consecutive keys (one 16-byte load) and the key before them, so every load
-// of the pass is independent and in flight at once. Tiles outside [0, tiles) can only come from a
-// timed-out sort; they are skipped.
-__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCtl* ctl, uint32_t tiles,
-                              uint32_t* __restrict__ ranges) {
-    pdl_wait();
-    const uint32_t n = ctl->sorted_count;
-    const uint32_t quads = (n + 3u) / 4u;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += gridDim.x * blockDim.x) {
-        const uint32_t i0 = q * 4u;
-        uint32_t k[4];
-        if (i0 + 4u <= n) {
-            const uint4 v = reinterpret_cast<const uint4*>(keys)[q];
-            k[0] = v.x; k[1] = v.y; k[2] = v.z; k[3] = v.w;
-        } else {
-#pragma unroll
-            for (uint32_t j = 0; j < 4u; ++j) k[j] = i0 + j < n ? keys[i0 + j] : 0u;
-        }
-        uint32_t prev = i0 ? keys[i0 - 1u] >> 16u : 0u;
-#pragma unroll
-        for (uint32_t j = 0; j < 4u; ++j) {
-            const uint32_t i = i0 + j;
-            if (i >= n) break;
-            const uint32_t tile = k[j] >> 16u;
-            if (tile < tiles) {
-                if (i == 0u) {
-                    ranges[tile * 2u] = 0u;
-                } else if (tile > prev && prev < tiles) {
-                    ranges[prev * 2u + 1u] = i;
-                    ranges[tile * 2u] = i;
+                if (ranges) {
+                    // last pass: the keys of one tile are contiguous in the CTA's local order (one digit
+                    // run, sorted by the lower bits), so the ends of each run of a tile give its range
+                    // bounds (tile_ranges.wgsl:7-34), combined over the CTAs by min / max
+                    const uint32_t tile = k >> 16u;
+                    if (tile < tiles) {
+                        if (i == 0u || (s_keys[i - 1u] >> 16u) != tile) atomicMin(&ranges[2u * tile], gpos);
+                        if (i + 1u == valid_n || (s_keys[i + 1u] >> 16u) != tile) atomicMax(&ranges[2u * tile + 1u], gpos + 1u);
+                    }
                 }
-                if (i == n - 1u) ranges[tile * 2u + 1u] = n;
             }
-            prev = tile;
         }
     }
 }
@@ -685,7 +660,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_bins(const uint32_t* __r
     if (threadIdx.x < 64u) slice_hist[blockIdx.x * 64u + threadIdx.x] = s_bin[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(kOrderThreads) k_tile_place(const uint32_t* __restrict__ ranges, uint32_t tiles,
+__global__ void __launch_bounds__(kOrderThreads) k_tile_place(uint32_t* __restrict__ ranges, uint32_t tiles,
                                                               const uint32_t* __restrict__ slice_hist,
                                                               uint32_t* __restrict__ order, uint32_t* status) {
     pdl_wait();
@@ -718,6 +693,8 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_place(const uint32_t* __
         if (t < tiles) {
             const uint32_t at = atomicAdd(&s_base[b[k]], 1u);
             if (GS_IN_BOUNDS(at, tiles, status)) order[at] = t;
+            // bin 63 is length 0: a tile the last sort pass left at its cleared bounds
+            if (b[k] == 63u) reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0u, 0u);
         }
     }
 }
@@ -804,7 +781,8 @@ void configure_sort_kernels() {
 void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
-                     int grid_cap, cudaStream_t s, uint32_t block, uint32_t split, bool early) {
+                     int grid_cap, cudaStream_t s, uint32_t block, uint32_t split, bool early, uint32_t* ranges,
+                     uint32_t tiles) {
     const bool small = block == kSortPartitionMin;
     const uint32_t part = small ? kSortPartitionMin : kSortPartition;
     uint32_t parts = (max_n + part - 1u) / part;
@@ -813,7 +791,7 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
     if (parts == 0) parts = 1;
 #define GS_ONESWEEP(B, I, S)                                                                                      \
     launch_pdl(k_onesweep<B, I, S>, dim3(parts), dim3(kSortThreads), s, keys_in, vals_in, keys_out, vals_out, n_dev, \
-               n_host, shift, dmask, hist, ctl, flags, slot, early ? 1u : 0u)
+               n_host, shift, dmask, hist, ctl, flags, slot, early ? 1u : 0u, ranges, tiles)
 #define GS_ONESWEEP_SPLIT(I)                             \
     switch (split) {                                     \
         case 2: GS_ONESWEEP(8, I, 2); break;             \
@@ -836,22 +814,13 @@ void launch_check_canaries(const CanaryList& list, uint32_t* status, cudaStream_
 
 uint32_t tile_order_slices(uint32_t tiles) { return (tiles + kOrderSlice - 1u) / kOrderSlice; }
 
-void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order,
-                       uint32_t* status, cudaStream_t s) {
+void launch_tile_order(uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order, uint32_t* status,
+                       cudaStream_t s) {
     const uint32_t slices = std::max(1u, tile_order_slices(tiles));
     launch_pdl(k_tile_bins, dim3(slices), dim3(kOrderThreads), s, ranges, tiles, slice_hist);
     launch_pdl(k_tile_place, dim3(slices), dim3(kOrderThreads), s, ranges, tiles, (const uint32_t*)slice_hist, order,
                status);
 }
 
-void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
-                        int grid_cap, cudaStream_t s) {
-    // one quad of keys per thread up to max_n keys, at most 16 CTAs per SM (grid-stride beyond)
-    uint32_t grid = (max_n / 4u + 255u) / 256u;
-    const uint32_t cap = grid_cap > 0 ? (uint32_t)grid_cap : (uint32_t)sm_count() * 16u;
-    if (grid > cap) grid = cap;
-    if (grid == 0) grid = 1;
-    launch_pdl(k_tile_ranges, dim3(grid), dim3(256), s, keys, ctl, tiles, ranges);
-}
 
 }  // namespace gs

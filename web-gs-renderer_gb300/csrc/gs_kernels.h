@@ -39,7 +39,8 @@ inline void launch_pdl(void (*k)(Params...), dim3 grid, dim3 block, cudaStream_t
 }
 
 // ---- frame ----------------------------------------------------------------------------------
-// Resets the frame control block and, when given, clears the frame's tile ranges (range_words words).
+// Resets the frame control block and, when given, clears the frame's tile ranges (range_words words,
+// every pair to (0xFFFFFFFF, 0): see launch_onesweep).
 // flags / flag_words: every lookback word the kernels of this control block use; they are cleared on
 // the one frame in 2^26 where the words' 30-bit sequence tags start again at zero.
 void launch_frame_begin(FrameCtl* ctl, uint64_t* flags, uint32_t flag_words, cudaStream_t s,
@@ -98,9 +99,13 @@ void launch_onesweep(uint32_t digit_bits, const uint32_t* keys_in, const uint32_
                      uint32_t* vals_out, const uint32_t* n_dev, uint32_t n_host, uint32_t max_n, uint32_t shift,
                      uint32_t dmask, const uint32_t* hist, FrameCtl* ctl, uint64_t* flags, uint32_t slot,
                      int grid_cap, cudaStream_t s, uint32_t block = kSortPartition, uint32_t split = 0,
-                     bool early = false);
+                     bool early = false, uint32_t* ranges = nullptr, uint32_t tiles = 0);
 // early: *n_dev (or n_host), hist, ctl->seq and the ticket counter were written at least two kernels
 // back on the stream, so they are read before the programmatic-launch wait for the previous kernel.
+// ranges (the last pass of a frame's sort only): each tile's (first, last + 1) in the sorted keys is
+// combined into ranges[2 tile], ranges[2 tile + 1] by atomic min / max over the CTAs; the ranges must
+// hold (0xFFFFFFFF, 0) before the pass (launch_frame_begin) and launch_tile_order, which reads them
+// next, puts (0, 0) into the tiles left empty.
 // Digit histograms of all passes over the low key_bits bits, for a standalone sort.
 void launch_digit_hist(const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t key_bits, uint32_t* hist,
                        cudaStream_t s);
@@ -113,8 +118,8 @@ void launch_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* total_dev, Fram
 // kernels over slices of 1024 tiles. slice_hist holds 64 words per slice (tile_order_slices), fully
 // rewritten by every call.
 uint32_t tile_order_slices(uint32_t tiles);
-void launch_tile_order(const uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order,
-                       uint32_t* status, cudaStream_t s);
+void launch_tile_order(uint32_t* ranges, uint32_t tiles, uint32_t* slice_hist, uint32_t* order, uint32_t* status,
+                       cudaStream_t s);
 
 // Checked builds: verifies the canary pads of up to kCanaryListMax buffers (head and tail pad of
 // kCanaryBytes each, filled with kCanaryWord) and sets kDevCanary in *status if any word changed.
@@ -128,8 +133,6 @@ struct CanaryList {
 };
 void launch_check_canaries(const CanaryList& list, uint32_t* status, cudaStream_t s);
 
-void launch_tile_ranges(const uint32_t* keys, const FrameCtl* ctl, uint32_t tiles, uint32_t* ranges, uint32_t max_n,
-                        int grid_cap, cudaStream_t s);
 
 struct RasterOut {
     uint32_t* rgba8;     // W*H packed rgba8 or null
