@@ -379,30 +379,35 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n, uint
 }
 
 // Sum of the values of `count` (1..7) tagged words p[0], p[-stride], ..., p[-(count-1) stride]: every
-// load is issued before the first is waited on; a word without this pass's tag is polled (bounded:
-// on expiry the timeout is recorded and the word counts as zero).
+// load is issued before the first is checked, and the words still without this pass's tag are polled
+// together (one memory round trip per poll for all of them), so the sum is ready one round trip after
+// the last of them is published. Bounded: on expiry the timeout is recorded and the words still
+// missing count as zero.
 __device__ __forceinline__ uint32_t sum_tagged(const uint64_t* p, size_t stride, uint32_t count, uint32_t want,
                                                uint32_t* status) {
     uint64_t w[7];
 #pragma unroll
     for (uint32_t q = 0; q < 7u; ++q) w[q] = q < count ? ld_relaxed_u64(p - q * stride) : 0ull;
+    auto ready = [&](uint64_t v) { return word_seq(v) == want && word_flag(v) != 0u; };
+    uint32_t spins = 0;
+    while (true) {
+        bool all = true;
+#pragma unroll
+        for (uint32_t q = 0; q < 7u; ++q) all = all && (q >= count || ready(w[q]));
+        if (all) break;
+        if (++spins > kSpinLimit) {
+            atomicOr(status, kDevTimeout);
+            break;
+        }
+        if (spins > 64u) __nanosleep(64);
+#pragma unroll
+        for (uint32_t q = 0; q < 7u; ++q)
+            if (q < count && !ready(w[q])) w[q] = ld_relaxed_u64(p - q * stride);
+    }
     uint32_t sum = 0;
 #pragma unroll
-    for (uint32_t q = 0; q < 7u; ++q) {
-        if (q >= count) break;
-        uint64_t v = w[q];
-        uint32_t spins = 0;
-        while (word_seq(v) != want || word_flag(v) == 0u) {
-            if (++spins > kSpinLimit) {
-                atomicOr(status, kDevTimeout);
-                v = make_word(want, kFlagAggregate, 0u);
-                break;
-            }
-            if (spins > 64u) __nanosleep(64);
-            v = ld_relaxed_u64(p - q * stride);
-        }
-        sum += word_value(v);
-    }
+    for (uint32_t q = 0; q < 7u; ++q)
+        if (q < count && ready(w[q])) sum += word_value(w[q]);
     return sum;
 }
 
@@ -460,6 +465,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t n = n_dev ? *n_dev : n_host;
     const uint32_t nparts = (n + PART - 1u) / PART;
+    // the grid is sized before n is known: CTAs past the partition count leave without taking a
+    // ticket (CTAs 0..nparts-1 take every partition between them, in ticket order), so they add no
+    // traffic on the ticket counter the working CTAs draw from
+    if (blockIdx.x >= nparts) return;
 
     if (tid == 0) s_seq = ctl->seq + slot;
     bool have_bases = false, waited = early == 0u;
