@@ -362,11 +362,6 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     if (profile) cudaEventRecord(ctx->ev[2], s);
     int cur = 0;
     const uint32_t key_bits = 16u + bitlen(a.tiles_x * a.tiles_y - 1u);
-    // the sort grid covers up to 8 instances per Gaussian (the scenes measured here carry 2-3): CTAs
-    // without a partition still cost a launch and a ticket each (with the grid sized for the 64N
-    // budget, a 100k-Gaussian view's 21 partitions shared their passes with ~590 idle CTAs, about
-    // 10 us per frame); past 8 per Gaussian the persistent CTAs take several partitions each
-    const uint32_t sort_span = (uint32_t)std::min<uint64_t>(a.max_instance, 8ull * a.n + kSortPartition);
     for (uint32_t p = 0; p < a.passes; ++p) {
         // the tile digits arrive in depth order, nearly all distinct within a warp: their ranking
         // matches the high half of the digit and separates the low half by ballots (w/2 of a w-bit
@@ -374,7 +369,7 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
         const uint32_t w = std::min(bits, key_bits - p * bits);
         const uint32_t split = p * bits >= 16u && w / 2u >= 2u ? w / 2u : 0u;
         launch_onesweep(bits, f.keys[cur].p, f.vals[cur].p, f.keys[cur ^ 1].p, f.vals[cur ^ 1].p, &ctl->sorted_count,
-                        0, sort_span, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
+                        0, a.max_instance, p * bits, radix - 1u, ctl->hist + p * radix, ctl, f.flags.p, 1 + p, 0, s,
                         ctx->cfg.sort_block, split, p > 0,  // the emit right before the first pass writes its inputs
                         p + 1 == a.passes ? f.ranges.p : nullptr, a.tiles_x * a.tiles_y);  // the last pass: ranges
         cur ^= 1;
