@@ -25,6 +25,36 @@ def test_sort_random_keys(gpu_ctx, n):
     np.testing.assert_array_equal(v, rv)
 
 
+def test_sort_deep_aggregate_tree(gpu_ctx):
+    """2^24 + 12,345 keys: 4,100 partitions of 4,096 keys, more than the 608 CTAs of a pass, so CTAs
+    take several partitions each and the per-digit prefixes of the last partitions come through
+    every level of the aggregate tree, a level-4 node (8^4 = 4,096 partitions) included."""
+    n = (1 << 24) + 12_345
+    rng = np.random.default_rng(24)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    k, v = gpu_ctx.sort_pairs(keys, vals, 32)
+    rk, rv = _stable_ref(keys, vals, 32)
+    np.testing.assert_array_equal(k, rk)
+    np.testing.assert_array_equal(v, rv)
+
+
+@pytest.mark.parametrize("digit_bits", [4, 8])
+def test_sort_small_partitions(digit_bits):
+    """The 2048-key partitions of the autotuner's smaller sort block: 1,465 partitions at 3M keys."""
+    import webgs
+
+    n = 3_000_000
+    rng = np.random.default_rng(2048 + digit_bits)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    with webgs.Context(digit_bits=digit_bits, sort_block=2048) as ctx:
+        k, v = ctx.sort_pairs(keys, vals, 32)
+    rk, rv = _stable_ref(keys, vals, 32)
+    np.testing.assert_array_equal(k, rk)
+    np.testing.assert_array_equal(v, rv)
+
+
 def test_sort_matches_literal_reference_radix(gpu_ctx):
     rng = np.random.default_rng(5)
     n = 70_000
