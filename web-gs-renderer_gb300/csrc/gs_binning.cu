@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
         for (uint32_t i = tid; i < valid_n; i += kSortThreads) {
             const uint32_t k = s_keys[i];
             const uint32_t gpos = s_out[(k >> shift) & MASK] + i;
-            if (gpos < n) {  // always true unless a lookback timed out (status already set)
+            if (gpos < n) {  // always true unless a wait on the tree timed out (status already set)
                 keys_out[gpos] = k;
                 vals_out[gpos] = s_vals[i];
                 if (ranges) {

@@ -70,7 +70,8 @@ void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uin
 void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
                        float4* rec, uint4* meta, uint32_t* counts, FrameCtl* ctl, cudaStream_t s);
 
-// Offset scan (decoupled lookback) fused with emit and the sort's digit histograms.
+// Offset scan (each partition sums its predecessors' published aggregates) fused with emit and the
+// sort's digit histograms.
 constexpr uint32_t kScanItems = 8;
 constexpr uint32_t kScanThreads = 256;
 constexpr uint32_t kScanPartition = kScanItems * kScanThreads;
