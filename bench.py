@@ -118,6 +118,8 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
     npass, vis, s = fi["near_pass"], fi["visible"], fi["sorted_count"]
     tiles = fi["tiles_x"] * fi["tiles_y"]
     return {
+        # the tile ranges cleared, the control block's counters and digit histograms reset
+        "frame begin": 8 * tiles + 8 * 1024,
         # 12 B position of every Gaussian + the other 224 B of each one in front of the near plane;
         # writes: 4 B count each, 48 B raster record per near-plane survivor, 16 B rect per visible
         "preprocess": 12 * n + 224 * npass + 4 * n + 48 * npass + 16 * vis,

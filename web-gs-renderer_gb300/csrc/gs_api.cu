@@ -79,8 +79,8 @@ uint32_t bitlen(uint32_t v) { return v == 0 ? 0u : 32u - (uint32_t)__builtin_clz
 
 constexpr int kViewSlots = 16;
 constexpr int kSideStreams = 16;
-enum Pass { kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
-const char* kPassLabel[kPassCount] = {"preprocess", "scan+emit", "sort", "tile order", "raster"};
+enum Pass { kPassBegin, kPassPreprocess, kPassScanEmit, kPassSort, kPassRanges, kPassRaster, kPassCount };
+const char* kPassLabel[kPassCount] = {"frame begin", "preprocess", "scan+emit", "sort", "tile order", "raster"};
 
 // Everything one view's frame needs on the device, and what the last frame on it was.
 struct Frame {
@@ -351,15 +351,16 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
     const uint32_t bits = ctx->cfg.digit_bits, radix = 1u << bits;
     FrameCtl* ctl = f.ctl.p;
     if (profile) cudaEventRecord(ctx->ev[0], s);
+    if (!preprocessed) launch_frame_begin(ctl, f.flags.p, (uint32_t)f.flags.cap, s, f.ranges.p, a.tiles_x * a.tiles_y * 2u);
+    if (profile) cudaEventRecord(ctx->ev[1], s);
     if (!preprocessed) {
-        launch_frame_begin(ctl, f.flags.p, (uint32_t)f.flags.cap, s, f.ranges.p, a.tiles_x * a.tiles_y * 2u);
         launch_preprocess(a.scene->rows, a.scene->stride, a.n, a.view, ctx->cfg.tile_size, f.rec.p, f.meta.p,
                           f.counts.p, ctl, s);
     }
-    if (profile) cudaEventRecord(ctx->ev[1], s);
+    if (profile) cudaEventRecord(ctx->ev[2], s);
     launch_scan_emit(f.counts.p, f.meta.p, a.n, a.tiles_x, a.max_instance, bits, a.passes, f.offsets.p, f.keys[0].p,
                      f.vals[0].p, ctl, f.flags.p, 0, s);
-    if (profile) cudaEventRecord(ctx->ev[2], s);
+    if (profile) cudaEventRecord(ctx->ev[3], s);
     int cur = 0;
     const uint32_t key_bits = 16u + bitlen(a.tiles_x * a.tiles_y - 1u);
     for (uint32_t p = 0; p < a.passes; ++p) {
@@ -374,12 +375,12 @@ void enqueue_frame(gs_ctx* ctx, Frame& f, const FrameArgs& a, cudaStream_t s, bo
                         p + 1 == a.passes ? f.ranges.p : nullptr, a.tiles_x * a.tiles_y);  // the last pass: ranges
         cur ^= 1;
     }
-    if (profile) cudaEventRecord(ctx->ev[3], s);
-    launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order_hist.p, f.order.p, &ctl->status, s);
     if (profile) cudaEventRecord(ctx->ev[4], s);
+    launch_tile_order(f.ranges.p, a.tiles_x * a.tiles_y, f.order_hist.p, f.order.p, &ctl->status, s);
+    if (profile) cudaEventRecord(ctx->ev[5], s);
     launch_raster(ctx->cfg.tile_size, ctx->cfg.raster_batch, f.ranges.p, f.vals[cur].p, f.rec.p, a.n, ctl, a.w, a.h,
                   a.tiles_x, a.tiles_y, a.out, f.order.p, s);
-    if (profile) cudaEventRecord(ctx->ev[5], s);
+    if (profile) cudaEventRecord(ctx->ev[6], s);
 }
 
 void remember(Frame& f, const FrameArgs& a) {
