@@ -28,8 +28,10 @@ namespace gs {
 // instructions, against 15 for the degree-7 Taylor form of the general pinned exp.
 // o = 0 (cut-off +inf) never gets here; for a NaN opacity the product o * exp(.) is NaN whatever this
 // returns, as with pinned_expf.
-__device__ __forceinline__ float raster_expf(float x) {
-    const float t = __fmaf_rn(x, 0x1.715476p+0f, 12582912.0f);
+// raster_exp_poly gives the two parts: it returns the polynomial p = e^r and sets t, whose low
+// mantissa bits hold n (e^x = p 2^n).
+__device__ __forceinline__ float raster_exp_poly(float x, float& t) {
+    t = __fmaf_rn(x, 0x1.715476p+0f, 12582912.0f);
     const float n = __fadd_rn(t, -12582912.0f);
     const float r = __fmaf_rn(-n, 0x1.62e43p-1f, x);
     float p = 0x1.6c350cp-10f;
@@ -38,8 +40,28 @@ __device__ __forceinline__ float raster_expf(float x) {
     p = __fmaf_rn(p, r, 0x1.55547ep-3f);
     p = __fmaf_rn(p, r, 0x1.fffffep-2f);
     p = __fmaf_rn(p, r, 1.0f);
-    p = __fmaf_rn(p, r, 1.0f);
+    return __fmaf_rn(p, r, 1.0f);
+}
+
+__device__ __forceinline__ float raster_expf(float x) {
+    float t;
+    const float p = raster_exp_poly(x, t);
     return __fmul_rn(p, __int_as_float((__float_as_int(t) + 127) << 23));
+}
+
+// o * raster_expf(x), bit for bit, for an argument at or above o's cut-off (x >= ln((1/255)/o) - 1e-3,
+// the only arguments the raster evaluates): raster_expf multiplies p by 2^n exactly, so o * (p 2^n)
+// rounds once, like (o p) 2^n, and scaling by 2^n commutes with rounding while nothing under- or
+// overflows. Above the cut-off o p 2^n is at least about 1/255 and o p at most about 1, all normal,
+// so 2^n is applied by adding n to the exponent field of o p: one integer op (the low bits of t hold
+// n; shifted up by 23 the rest of t falls off) instead of building 2^n and a second multiply (raster
+// of the 1M / 1080p frame 0.2621 -> 0.2583 ms). A NaN argument or opacity gives the canonical NaN in
+// o p (or, for a NaN opacity, a large finite value after the add), which min(0.99, .) turns into
+// 0.99, as it does the NaN of o * raster_expf.
+__device__ __forceinline__ float raster_alpha_unclamped(float o, float x) {
+    float t;
+    const float p = raster_exp_poly(x, t);
+    return __int_as_float(__float_as_int(__fmul_rn(o, p)) + (__float_as_int(t) << 23));
 }
 
 __device__ __forceinline__ bool finite_f(float v) { return fabsf(v) <= 3.0e38f; }
