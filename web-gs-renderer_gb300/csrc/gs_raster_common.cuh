@@ -55,9 +55,9 @@ __device__ __forceinline__ float raster_expf(float x) {
 // overflows. Above the cut-off o p 2^n is at least about 1/255 and o p at most about 1, all normal,
 // so 2^n is applied by adding n to the exponent field of o p: one integer op (the low bits of t hold
 // n; shifted up by 23 the rest of t falls off) instead of building 2^n and a second multiply (raster
-// of the 1M / 1080p frame 0.2621 -> 0.2583 ms). A NaN argument or opacity gives the canonical NaN in
-// o p (or, for a NaN opacity, a large finite value after the add), which min(0.99, .) turns into
-// 0.99, as it does the NaN of o * raster_expf.
+// of the 1M / 1080p frame 0.2621 -> 0.2583 ms). Where o p is NaN (a NaN argument or opacity) it is
+// the GPU's positive canonical NaN, which the add leaves a NaN or turns into a large positive finite
+// value; min(0.99, .) makes 0.99 of either, as it does of the NaN of o * raster_expf.
 __device__ __forceinline__ float raster_alpha_unclamped(float o, float x) {
     float t;
     const float p = raster_exp_poly(x, t);
