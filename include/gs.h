@@ -274,6 +274,10 @@ int gs_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t locati
 /* The raster's pinned exp (alpha = o * exp(power), raseter.wgsl:89), defined for x in [-5.6, 0], on
  * the device: for parity tests against the oracle. */
 int gs_raster_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t location);
+/* y = o * exp(x) before the 0.99 clamp, formed on the device as the raster forms it (raseter.wgsl:89),
+ * for x at or above o's cut-off ln((1/255)/o) - 1e-3 (the only arguments the raster evaluates): for
+ * parity tests against the oracle's o * raster_expf(x). o, x and y hold n floats each. */
+int gs_raster_alpha_f32(gs_ctx* ctx, const float* o, const float* x, float* y, uint32_t n, int32_t location);
 
 /* Exclusive scan for callers that must not allocate device memory (no counterpart in the
  * reference). Same result as gs_exclusive_scan, but it needs no context and calls no cudaMalloc,

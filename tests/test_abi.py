@@ -148,5 +148,6 @@ def test_new_entry_points_reject_null_context():
     assert lib.gs_camera_views(None, None, 0, None, webgs.GS_MEM_HOST) == _abi.GS_ERR_INVALID
     assert lib.gs_forward_batch_cameras(None, None, 1) == _abi.GS_ERR_INVALID
     assert lib.gs_raster_exp_f32(None, None, None, 0, webgs.GS_MEM_HOST) == _abi.GS_ERR_INVALID
+    assert lib.gs_raster_alpha_f32(None, None, None, None, 0, webgs.GS_MEM_HOST) == _abi.GS_ERR_INVALID
     assert lib.gs_debug_set_sequence is not None  # a test hook (needs a GPU to do anything)
     assert C.sizeof(_abi.Camera) == 56 and C.sizeof(_abi.BatchCamera) == C.sizeof(_abi.BatchView) - 176 + 56

@@ -1,5 +1,6 @@
 """Building blocks on the GPU vs the oracle: the radix sort (gs_sort_pairs), the decoupled-lookback
-scan (gs_exclusive_scan) and the pinned exp (gs_exp_f32), through the C ABI."""
+scan (gs_exclusive_scan), the pinned exps (gs_exp_f32, gs_raster_exp_f32) and the raster's
+o * exp(power) (gs_raster_alpha_f32), through the C ABI."""
 import numpy as np
 import pytest
 
@@ -111,3 +112,31 @@ def test_raster_exp_bitwise(gpu_ctx):
     g = gpu_ctx.exp(x, raster=True)
     o = oracle.raster_expf(x)
     np.testing.assert_array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_raster_alpha_bitwise(gpu_ctx):
+    """o * exp(power) as the raster forms it (2^n added to the exponent field of o * p) equals the
+    oracle's o * raster_expf(power) bit for bit, for every power the raster evaluates: at or above the
+    opacity's cut-off ln((1/255)/o) - 1e-3 (an opacity below about 1/255 has a positive cut-off and is
+    never evaluated). NaN opacities or powers give 0.99 after the clamp, as the oracle's NaN does."""
+    rng = np.random.default_rng(7)
+    n = 3_000_000
+    lo = np.float32(1.0 / 255.0) * np.float32(1.01)
+    o = rng.uniform(float(lo), 1.0, n).astype(np.float32)
+    o[:1000] = 1.0
+    o[1000:2000] = lo
+    cut = (np.log((1.0 / 255.0) / o.astype(np.float64)) - 1e-3).astype(np.float32)
+    x = (cut.astype(np.float64) * rng.uniform(0.0, 1.0, n)).astype(np.float32)  # in (cut, 0]
+    x[2000:3000] = np.float32(0.0)
+    x[3000:4000] = np.float32(-0.0)
+    x[4000:5000] = (cut[4000:5000].astype(np.float64) * (1.0 - 1e-6)).astype(np.float32)
+    y = gpu_ctx.raster_alpha(o, x)
+    ref = o * oracle.raster_expf(x)
+    np.testing.assert_array_equal(y.view(np.uint32), ref.view(np.uint32))
+    nan = np.float32(np.nan)
+    on = np.array([nan, 0.5, nan, 0.0], np.float32)
+    xn = np.array([-1.0, nan, nan, nan], np.float32)
+    yn = np.fmin(np.float32(0.99), gpu_ctx.raster_alpha(on, xn))
+    rn = np.fmin(np.float32(0.99), on * oracle.raster_expf(xn))
+    np.testing.assert_array_equal(yn, rn)
+    assert (yn == np.float32(0.99)).all()

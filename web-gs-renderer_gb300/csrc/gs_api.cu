@@ -1433,4 +1433,29 @@ int gs_raster_exp_f32(gs_ctx* ctx, const float* x, float* y, uint32_t n, int32_t
     return exp_f32(ctx, x, y, n, location, true);
 }
 
+int gs_raster_alpha_f32(gs_ctx* ctx, const float* o, const float* x, float* y, uint32_t n, int32_t location) {
+    if (!ctx) return GS_ERR_INVALID;
+    if ((!o || !x || !y) && n) return fail(ctx, GS_ERR_INVALID, "gs_raster_alpha_f32: null buffer");
+    if (location != GS_MEM_HOST && location != GS_MEM_DEVICE)
+        return fail(ctx, GS_ERR_INVALID, "gs_raster_alpha_f32: bad location");
+    if (n == 0) return GS_OK;
+    GS_CK(cudaSetDevice(ctx->cfg.device));
+    if (location == GS_MEM_DEVICE) {
+        launch_raster_alpha(o, x, y, n, ctx->stream);
+        GS_CK(cudaGetLastError());
+        return GS_OK;
+    }
+    GS_CK(ctx->aux_f32.reserve((size_t)n * 3));
+    float* d_o = ctx->aux_f32.p;
+    float* d_x = d_o + n;
+    float* d_y = d_x + n;
+    GS_CK(cudaMemcpyAsync(d_o, o, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    GS_CK(cudaMemcpyAsync(d_x, x, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    launch_raster_alpha(d_o, d_x, d_y, n, ctx->stream);
+    GS_CK(cudaGetLastError());
+    GS_CK(cudaMemcpyAsync(y, d_y, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GS_CK(cudaStreamSynchronize(ctx->stream));
+    return GS_OK;
+}
+
 }  // extern "C"

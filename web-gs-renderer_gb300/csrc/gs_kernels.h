@@ -149,6 +149,8 @@ void launch_raster(uint32_t tile, uint32_t batch, const uint32_t* ranges, const 
 
 // y = the pinned exp of x (raster: the raster's exp, defined on [-5.6, 0]).
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s, bool raster = false);
+// y = o * exp(x) as the raster forms it, before the 0.99 clamp (x at or above o's cut-off).
+void launch_raster_alpha(const float* o, const float* x, float* y, uint32_t n, cudaStream_t s);
 
 }  // namespace gs
 struct gs_camera;

@@ -383,6 +383,12 @@ __global__ void k_exp(const float* __restrict__ x, float* __restrict__ y, uint32
     if (i < n) y[i] = RASTER ? raster_expf(x[i]) : pinned_expf(x[i]);
 }
 
+__global__ void k_raster_alpha(const float* __restrict__ o, const float* __restrict__ x, float* __restrict__ y,
+                               uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = raster_alpha_unclamped(o[i], x[i]);
+}
+
 }  // namespace
 
 void launch_preprocess(const float* rows, uint32_t stride, uint32_t n, const ViewBlock* view, uint32_t tile,
@@ -403,6 +409,11 @@ void launch_preprocess_multi(const float* rows, uint32_t stride, uint32_t n, uin
 void launch_pack_to_rows(const float* packed, uint32_t n, uint32_t stride, float* rows, cudaStream_t s) {
     dim3 grid((stride + kTransposeGroup - 1u) / kTransposeGroup, 6);
     k_pack_to_rows<<<grid, 256, 0, s>>>(packed, n, stride, rows);
+}
+
+void launch_raster_alpha(const float* o, const float* x, float* y, uint32_t n, cudaStream_t s) {
+    if (n == 0) return;
+    k_raster_alpha<<<(n + 255u) / 256u, 256, 0, s>>>(o, x, y, n);
 }
 
 void launch_exp(const float* x, float* y, uint32_t n, cudaStream_t s, bool raster) {

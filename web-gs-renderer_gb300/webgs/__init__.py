@@ -374,6 +374,16 @@ class Context:
         self._ck(fn(self.handle, _ptr(xx), _ptr(y), xx.size, GS_MEM_HOST))
         return y
 
+    def raster_alpha(self, o: np.ndarray, x: np.ndarray) -> np.ndarray:
+        """o * exp(x) as the raster forms it, before the 0.99 clamp (x at or above o's cut-off)."""
+        oo = np.ascontiguousarray(o, dtype=np.float32)
+        xx = np.ascontiguousarray(x, dtype=np.float32)
+        if oo.shape != xx.shape:
+            raise ValueError("raster_alpha: o and x differ in shape")
+        y = np.empty_like(xx)
+        self._ck(library().gs_raster_alpha_f32(self.handle, _ptr(oo), _ptr(xx), _ptr(y), xx.size, GS_MEM_HOST))
+        return y
+
 
 def _forward_tracking(fn):
     def wrapper(self, scene, *a, **k):

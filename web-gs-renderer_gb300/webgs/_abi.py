@@ -137,6 +137,7 @@ SIGNATURES = [
     ("gs_exclusive_scan", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]),
     ("gs_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
     ("gs_raster_exp_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
+    ("gs_raster_alpha_f32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32]),
     ("gs_check_wait_timeout", C.c_int, [C.c_void_p]),
     ("gs_exclusive_scan_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("gs_debug_set_sequence", C.c_int, [C.c_void_p, C.c_uint32]),
