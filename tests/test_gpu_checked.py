@@ -31,8 +31,14 @@ def _env():
     return env
 
 
+# Timing comparisons are left to the product build: the checked build's bounds checks change the
+# kernels' speed, and a test that the autotuner's pick is no slower than the defaults measures nothing
+# about stores or pads.
+TIMING_TESTS = "not autotune_pick_is_not_slower_than_the_defaults"
+
+
 def test_parity_suites_pass_under_the_checked_build():
-    cmd = [sys.executable, "-m", "pytest", "-m", "gpu", "-x", "-q", "-p", "no:cacheprovider",
+    cmd = [sys.executable, "-m", "pytest", "-m", "gpu", "-x", "-q", "-p", "no:cacheprovider", "-k", TIMING_TESTS,
            *[str(ROOT / "tests" / f) for f in SUITES]]
     proc = subprocess.run(cmd, cwd=ROOT, env=_env(), capture_output=True, text=True, timeout=1800)
     assert proc.returncode == 0, proc.stdout[-4000:] + proc.stderr[-2000:]
