@@ -139,12 +139,12 @@ def algorithmic_bytes(fi: dict, n: int, pixels: int, passes: int) -> dict:
 NCU_TRAFFIC_BYTES = {"preprocess": 286.5e6, "raster": 56.6e6}
 # issue-slot utilisation of the kernels bound by instruction issue (ncu smsp__issue_active, one
 # capture of the kernel at this workload): for them this, not the HBM fraction, is the efficiency measure
-NCU_ISSUE_ACTIVE = {"raster": 0.936}
+NCU_ISSUE_ACTIVE = {"raster": 0.933}
 # warp instructions per launch (ncu smsp__inst_executed.sum, the same capture): the numerator of the
 # issue-rate roofline of those kernels (four issue slots per SM per cycle)
-NCU_WARP_INSTRUCTIONS = {"raster": 287.70e6}
+NCU_WARP_INSTRUCTIONS = {"raster": 275.27e6}
 LIMITER = {
-    "raster": "instruction issue (ncu: issue slots busy 93.6% at full residency, DRAM 3% of peak; the "
+    "raster": "instruction issue (ncu: issue slots busy 93.3% at full residency, DRAM 3% of peak; the "
               "48-byte records are re-read from L2, so DRAM traffic is below the algorithmic bytes)",
     "preprocess": "HBM and the pinned arithmetic (ncu: 69% of DRAM peak, 70% of issue slots)",
 }
