@@ -89,7 +89,7 @@ float raster_expf(float x) {
 }
 
 // The raster's alpha exp over every argument the WGSL evaluates it at (power <= 0). The CUDA raster
-// evaluates it only from the splat's cut-off up (power >= ln((1/255)/o) - 1e-3 > -5.6 for any o in
+// uses it only from the splat's cut-off up (power >= ln((1/255)/o) - 1e-3 > -5.6 for any o in
 // [0, 1]; a pixel below skips, its alpha being below 1/255 for sure); here raster_expf covers
 // [-5.6, 0] and the general pinned exp the arguments below, where any value keeps alpha below 1/255
 // and so gives the same skip. (A NaN opacity makes alpha 0.99 whatever exp returns, in both.)
