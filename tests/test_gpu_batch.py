@@ -131,8 +131,10 @@ def test_autotune_pick_is_not_slower_than_the_defaults():
     cams = [(i % 2, c) for i, (_, c) in enumerate(W.orbit_cameras(6, 31, 9.0))]
     cfg, _ = webgs.autotune_scenes([(p, s.count) for s, p in zip(specs, packs)], [c.view() for _, c in cams],
                                    [si for si, _ in cams], iters=3)
-    tuned = _batch_ms(cfg, (specs, cams), packs)
-    default = _batch_ms({}, (specs, cams), packs)
+    # interleaved, the best of two each, so that a drift of the clock between the two does not land
+    # on one side only
+    runs = [_batch_ms(c, (specs, cams), packs) for c in (cfg, {}, cfg, {})]
+    tuned, default = min(runs[0::2]), min(runs[1::2])
     assert tuned <= default * 1.05, (cfg, tuned, default)
 
 
